@@ -1,0 +1,688 @@
+// C ABI of the batched rigid-body step (declared in include/cubez_gpu.h).
+//
+// A batch owns every device buffer it uses (allocated once in
+// cz_batch_create), one non-blocking CUDA stream, and a cache of captured
+// CUDA graphs for multi-step rollouts.  Calls on one batch are serialised by
+// the caller (the reference is single-threaded, contact.go has no locking).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <numeric>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "../../include/cubez_gpu.h"
+#include "cz_forms.h"
+#include "cz_layout.cuh"
+
+namespace {
+
+thread_local std::string g_last_error;
+std::atomic<long long> g_launches{0};
+
+int fail(int status, const std::string& msg) {
+  g_last_error = msg;
+  return status;
+}
+
+#define CZ_CUDA(call)                                                                                   \
+  do {                                                                                                  \
+    cudaError_t e_ = (call);                                                                            \
+    if (e_ != cudaSuccess)                                                                              \
+      return fail(CZ_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));                    \
+  } while (0)
+
+long long round_up(long long x, long long m) { return (x + m - 1) / m * m; }
+
+}  // namespace
+
+struct cz_batch {
+  const cz::FormOps* ops = nullptr;
+  int form = 0;
+  int device = 0;
+  int sm_count = 0;
+  size_t smem_optin = 0;
+  cudaStream_t stream = nullptr;
+
+  int num_worlds = 0;
+  long long nb = 0, nb_pad = 0, nc_total = 0;
+  std::vector<int> counts, bstart, ccap, h2p;
+  std::vector<long long> cstart;
+  int max_n = 0, nbs = 4, max_cap = 1;
+
+  // device buffers
+  void* body = nullptr;
+  uint8_t* awake = nullptr;
+  uint8_t* can_sleep = nullptr;
+  int* shape = nullptr;
+  int *d_bstart = nullptr, *d_bcount = nullptr, *d_ccap = nullptr, *d_ccount = nullptr;
+  long long* d_cstart = nullptr;
+  uint32_t* d_wstatus = nullptr;
+  int *d_piters = nullptr, *d_viters = nullptr;
+  void* contact = nullptr;
+  int* cbodies = nullptr;
+  void* work = nullptr;
+  int* wbodies = nullptr;
+  int* d_order = nullptr;
+  unsigned* d_queue = nullptr;
+  uint32_t* d_status = nullptr;
+  int* d_h2p = nullptr;
+  double* d_stage = nullptr;
+  uint8_t* d_stage_u8 = nullptr;
+  int* d_stage_i32 = nullptr;
+  double* d_cstage = nullptr;
+  int* d_cstage_b = nullptr;
+  double* d_pow = nullptr;
+  // pinned host staging
+  double* h_stage = nullptr;
+  uint8_t* h_stage_u8 = nullptr;
+  int* h_stage_i32 = nullptr;
+  double* h_cstage = nullptr;
+  int* h_cstage_b = nullptr;
+  double* h_pow = nullptr;
+  uint32_t* h_status = nullptr;
+
+  std::vector<double> lin_damp, ang_damp;
+  double pow_dt = std::nan("");
+  double plane[4] = {0, 1, 0, 0};
+  int iter_mult = 4;
+  int max_iterations = -1;
+
+  // tuning
+  int np_threads = 128, np_grid = 1, rs_cs = 128, rs_grid = 1, rs_ctas_per_sm = 0, int_threads = 256;
+  size_t np_smem = 0, rs_smem = 0;
+
+  // graph cache: (nsteps, dt) -> executable graph
+  std::map<std::pair<int, double>, cudaGraphExec_t> graphs;
+
+  cz::HostView view() const {
+    cz::HostView v;
+    v.body = body;
+    v.awake = awake;
+    v.can_sleep = can_sleep;
+    v.shape = shape;
+    v.nb_pad = nb_pad;
+    v.num_worlds = num_worlds;
+    v.max_bodies = max_n;
+    v.body_start = d_bstart;
+    v.body_count = d_bcount;
+    v.contact_start = d_cstart;
+    v.contact_cap = d_ccap;
+    v.contact_count = d_ccount;
+    v.world_status = d_wstatus;
+    v.pos_iters = d_piters;
+    v.vel_iters = d_viters;
+    v.contact = contact;
+    v.contact_bodies = cbodies;
+    v.work = work;
+    v.work_bodies = wbodies;
+    v.nc_total = nc_total;
+    v.order = d_order;
+    v.queue = d_queue;
+    v.status = d_status;
+    for (int i = 0; i < 4; ++i) v.plane[i] = plane[i];
+    v.iter_mult = iter_mult;
+    v.max_iterations = max_iterations;
+    v.contact_writeback = 0;
+    return v;
+  }
+};
+
+namespace {
+
+void free_batch(cz_batch* b) {
+  if (!b) return;
+  cudaSetDevice(b->device);
+  for (auto& kv : b->graphs) cudaGraphExecDestroy(kv.second);
+  void* dev[] = {b->body, b->awake, b->can_sleep, b->shape, b->d_bstart, b->d_bcount, b->d_ccap, b->d_ccount,
+                 b->d_cstart, b->d_wstatus, b->d_piters, b->d_viters, b->contact, b->cbodies, b->work, b->wbodies,
+                 b->d_order, b->d_queue, b->d_status, b->d_h2p, b->d_stage, b->d_stage_u8, b->d_stage_i32,
+                 b->d_cstage, b->d_cstage_b, b->d_pow};
+  for (void* p : dev)
+    if (p) cudaFree(p);
+  void* host[] = {b->h_stage, b->h_stage_u8, b->h_stage_i32, b->h_cstage, b->h_cstage_b, b->h_pow, b->h_status};
+  for (void* p : host)
+    if (p) cudaFreeHost(p);
+  if (b->stream) cudaStreamDestroy(b->stream);
+  delete b;
+}
+
+int status_from_bits(uint32_t bits) {
+  if (bits & cz::ST_TIMEOUT) return CZ_ERR_TIMEOUT;
+  if (bits & cz::ST_NONFINITE) return CZ_ERR_NONFINITE;
+  if (bits & cz::ST_CAPACITY) return CZ_ERR_CAPACITY;
+  if (bits & cz::ST_BODY_LIMIT) return CZ_ERR_BODY_LIMIT;
+  if (bits & cz::ST_FRICTIONLESS_NIL) return CZ_ERR_FRICTIONLESS;
+  return CZ_OK;
+}
+
+// Synchronise the batch stream and turn the device status word into a cz_status.
+int finish(cz_batch* b) {
+  CZ_CUDA(cudaMemcpyAsync(b->h_status, b->d_status, sizeof(uint32_t), cudaMemcpyDeviceToHost, b->stream));
+  CZ_CUDA(cudaStreamSynchronize(b->stream));
+  const uint32_t bits = *b->h_status;
+  const int st = status_from_bits(bits);
+  if (st != CZ_OK) {
+    char buf[96];
+    std::snprintf(buf, sizeof buf, "device status bits 0x%x", bits);
+    g_last_error = buf;
+  }
+  return st;
+}
+
+int reset_status(cz_batch* b) {
+  CZ_CUDA(cudaMemsetAsync(b->d_status, 0, sizeof(uint32_t), b->stream));
+  return CZ_OK;
+}
+
+// pow(LinearDamping, dt) and pow(AngularDamping, dt) per body, computed on the
+// host (math.Pow in the reference, rigidbody.go:233-234).
+int ensure_pows(cz_batch* b, double dt) {
+  if (b->pow_dt == dt) return CZ_OK;
+  const long long P = b->nb_pad;
+  for (long long i = 0; i < 2 * P; ++i) b->h_pow[i] = 1.0;
+  for (long long h = 0; h < b->nb; ++h) {
+    const long long p = b->h2p[h];
+    b->h_pow[p] = std::pow(b->lin_damp[h], dt);
+    b->h_pow[P + p] = std::pow(b->ang_damp[h], dt);
+  }
+  CZ_CUDA(cudaMemcpyAsync(b->d_pow, b->h_pow, sizeof(double) * 2 * P, cudaMemcpyHostToDevice, b->stream));
+  CZ_CUDA(b->ops->set_rows(b->view(), cz::B_LINPOW, 2, b->d_pow, b->stream));
+  g_launches++;
+  CZ_CUDA(cudaStreamSynchronize(b->stream));
+  b->pow_dt = dt;
+  return CZ_OK;
+}
+
+int launch_integrate(cz_batch* b, double dt) {
+  CZ_CUDA(b->ops->integrate(b->view(), dt, std::pow(0.5, dt), b->int_threads, b->stream));
+  g_launches++;
+  return CZ_OK;
+}
+int launch_narrowphase(cz_batch* b) {
+  CZ_CUDA(cudaMemsetAsync(b->d_queue, 0, sizeof(unsigned), b->stream));
+  CZ_CUDA(b->ops->narrowphase(b->view(), b->nbs, b->np_threads, b->np_grid, b->np_smem, b->stream));
+  g_launches++;
+  return CZ_OK;
+}
+int launch_resolve(cz_batch* b, double dt, const cz::HostView* override_view = nullptr) {
+  CZ_CUDA(cudaMemsetAsync(b->d_queue + 1, 0, sizeof(unsigned), b->stream));
+  CZ_CUDA(b->ops->resolve(override_view ? *override_view : b->view(), b->nbs, b->rs_cs, b->rs_grid, b->rs_smem, dt,
+                          b->stream));
+  g_launches++;
+  return CZ_OK;
+}
+
+int configure(cz_batch* b) {
+  // resolver shared-memory tile: shrink the contact capacity until it fits
+  int cs = std::min<long long>(b->rs_cs, round_up(b->max_cap, 32));
+  cs = std::max(cs, 32);
+  while (cs > 32 && b->ops->rs_smem(b->nbs, cs) > b->smem_optin) cs -= 32;
+  b->rs_cs = cs;
+  b->rs_smem = b->ops->rs_smem(b->nbs, cs);
+  b->np_smem = b->ops->np_smem(b->nbs);
+  if (b->np_smem > b->smem_optin || b->rs_smem > b->smem_optin)
+    return fail(CZ_ERR_BODY_LIMIT, "world too large for the shared-memory tiles");
+  CZ_CUDA(b->ops->prepare(b->np_smem, b->rs_smem));
+  int npb = 0, rsb = 0;
+  CZ_CUDA(b->ops->occupancy(&npb, b->np_threads, b->np_smem, &rsb, b->rs_smem));
+  npb = std::max(npb, 1);
+  rsb = std::max(rsb, 1);
+  if (b->rs_ctas_per_sm > 0) rsb = std::min(rsb, b->rs_ctas_per_sm);
+  b->np_grid = (int)std::min<long long>(b->num_worlds, (long long)npb * b->sm_count);
+  b->rs_grid = (int)std::min<long long>(b->num_worlds, (long long)rsb * b->sm_count);
+  b->np_grid = std::max(b->np_grid, 1);
+  b->rs_grid = std::max(b->rs_grid, 1);
+  for (auto& kv : b->graphs) cudaGraphExecDestroy(kv.second);
+  b->graphs.clear();
+  return CZ_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* cz_status_string(int status) {
+  switch (status) {
+    case CZ_OK: return "ok";
+    case CZ_ERR_BAD_ARG: return "bad argument";
+    case CZ_ERR_CUDA: return "CUDA error";
+    case CZ_ERR_NO_DEVICE: return "no CUDA device";
+    case CZ_ERR_NONFINITE: return "non-finite box transform in the box-box test";
+    case CZ_ERR_CAPACITY: return "contact capacity exceeded";
+    case CZ_ERR_TIMEOUT: return "device wait timed out";
+    case CZ_ERR_FRICTIONLESS: return "frictionless impulse on a single-body contact";
+    case CZ_ERR_BODY_LIMIT: return "world too large for the kernel tiles";
+    default: return "unknown status";
+  }
+}
+
+const char* cz_last_error(void) { return g_last_error.c_str(); }
+
+int64_t cz_kernel_launches(void) { return g_launches.load(); }
+
+int cz_batch_create(const cz_batch_desc* d, cz_batch** out) {
+  if (!d || !out || d->num_worlds <= 0 || !d->body_counts || (d->form != CZ_FORM_FP64 && d->form != CZ_FORM_FP32))
+    return fail(CZ_ERR_BAD_ARG, "cz_batch_create: bad descriptor");
+  *out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0) return fail(CZ_ERR_NO_DEVICE, "no CUDA device");
+  if (d->device < 0 || d->device >= ndev) return fail(CZ_ERR_BAD_ARG, "cz_batch_create: bad device ordinal");
+  for (int w = 0; w < d->num_worlds; ++w)
+    if (d->body_counts[w] < 0 || d->body_counts[w] >= 65535)
+      return fail(CZ_ERR_BAD_ARG, "cz_batch_create: body count out of range");
+  cz_batch* b = new cz_batch();
+  b->form = d->form;
+  b->ops = d->form == CZ_FORM_FP64 ? &cz::kFormFP64 : &cz::kFormFP32;
+  b->device = d->device;
+  int st = CZ_OK;
+  auto bail = [&](int s) {
+    free_batch(b);
+    return s;
+  };
+  if (cudaSetDevice(b->device) != cudaSuccess) return bail(fail(CZ_ERR_CUDA, "cudaSetDevice failed"));
+  cudaDeviceGetAttribute(&b->sm_count, cudaDevAttrMultiProcessorCount, b->device);
+  int optin = 0;
+  cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, b->device);
+  b->smem_optin = (size_t)optin;
+  b->num_worlds = d->num_worlds;
+  b->counts.assign(d->body_counts, d->body_counts + d->num_worlds);
+  for (int i = 0; i < 3; ++i) b->plane[i] = d->plane[i];
+  b->plane[3] = d->plane[3];
+  if (d->plane[0] == 0 && d->plane[1] == 0 && d->plane[2] == 0) {
+    b->plane[0] = 0; b->plane[1] = 1; b->plane[2] = 0;
+  }
+  b->iter_mult = d->iteration_multiplier > 0 ? d->iteration_multiplier : 4;
+  b->max_iterations = d->max_iterations > 0 ? d->max_iterations : -1;
+  // layout
+  long long nb = 0, np = 0, nc = 0;
+  for (int w = 0; w < b->num_worlds; ++w) {
+    const int n = b->counts[w];
+    b->bstart.push_back((int)np);
+    for (int i = 0; i < n; ++i) b->h2p.push_back((int)(np + i));
+    np = round_up(np + n, 4);
+    nb += n;
+    b->max_n = std::max(b->max_n, n);
+    const long long worst = 8LL * n + (long long)n * (n - 1);
+    long long cap = std::min<long long>(worst, std::max<long long>(64LL * n, 4608));
+    if (d->contact_capacity > 0) cap = std::min<long long>(worst, d->contact_capacity);
+    cap = std::max<long long>(cap, 1);
+    b->ccap.push_back((int)cap);
+    b->cstart.push_back(nc);
+    nc += round_up(cap, 4);
+    b->max_cap = std::max<int>(b->max_cap, (int)cap);
+  }
+  b->nb = nb;
+  b->nb_pad = std::max<long long>(np, 4);
+  b->nc_total = std::max<long long>(nc, 4);
+  b->nbs = (int)std::max<long long>(round_up(b->max_n, 4), 4);
+  b->np_threads = b->max_n >= 256 ? 256 : 128;
+  b->rs_cs = d->form == CZ_FORM_FP64 ? 128 : 192;
+  // world queue: decreasing body count (pair work grows as n^2)
+  std::vector<int> order(b->num_worlds);
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(), [&](int a, int c) { return b->counts[a] > b->counts[c]; });
+
+  const size_t R = b->ops->real_size;
+  const long long P = b->nb_pad, C = b->nc_total, W = b->num_worlds;
+  auto dmalloc = [&](void** p, size_t bytes) -> bool {
+    if (cudaMalloc(p, std::max<size_t>(bytes, 16)) != cudaSuccess) return false;
+    return true;
+  };
+  bool ok = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) == cudaSuccess;
+  ok = ok && dmalloc(&b->body, R * cz::B_NROWS * P);
+  ok = ok && dmalloc((void**)&b->awake, P) && dmalloc((void**)&b->can_sleep, P) &&
+       dmalloc((void**)&b->shape, sizeof(int) * P);
+  ok = ok && dmalloc((void**)&b->d_bstart, sizeof(int) * W) && dmalloc((void**)&b->d_bcount, sizeof(int) * W) &&
+       dmalloc((void**)&b->d_ccap, sizeof(int) * W) && dmalloc((void**)&b->d_ccount, sizeof(int) * W) &&
+       dmalloc((void**)&b->d_cstart, sizeof(long long) * W) && dmalloc((void**)&b->d_wstatus, sizeof(uint32_t) * W) &&
+       dmalloc((void**)&b->d_piters, sizeof(int) * W) && dmalloc((void**)&b->d_viters, sizeof(int) * W) &&
+       dmalloc((void**)&b->d_order, sizeof(int) * W);
+  ok = ok && dmalloc(&b->contact, R * cz::C_NROWS * C) && dmalloc((void**)&b->cbodies, sizeof(int) * C);
+  ok = ok && dmalloc(&b->work, R * cz::W_NROWS * C) && dmalloc((void**)&b->wbodies, sizeof(int) * C);
+  ok = ok && dmalloc((void**)&b->d_queue, 4 * sizeof(unsigned)) && dmalloc((void**)&b->d_status, sizeof(uint32_t));
+  ok = ok && dmalloc((void**)&b->d_h2p, sizeof(int) * std::max<long long>(nb, 1));
+  ok = ok && dmalloc((void**)&b->d_stage, sizeof(double) * cz::SG_NDOUBLES * std::max<long long>(nb, 1)) &&
+       dmalloc((void**)&b->d_stage_u8, 2 * std::max<long long>(nb, 1)) &&
+       dmalloc((void**)&b->d_stage_i32, sizeof(int) * std::max<long long>(nb, 1));
+  ok = ok && dmalloc((void**)&b->d_cstage, sizeof(double) * cz::C_NROWS * b->max_cap) &&
+       dmalloc((void**)&b->d_cstage_b, sizeof(int) * b->max_cap);
+  ok = ok && dmalloc((void**)&b->d_pow, sizeof(double) * 2 * P);
+  if (!ok) return bail(fail(CZ_ERR_CUDA, "device allocation failed"));
+  ok = cudaMallocHost((void**)&b->h_stage, sizeof(double) * cz::SG_NDOUBLES * std::max<long long>(nb, 1)) ==
+           cudaSuccess &&
+       cudaMallocHost((void**)&b->h_stage_u8, 2 * std::max<long long>(nb, 1)) == cudaSuccess &&
+       cudaMallocHost((void**)&b->h_stage_i32, sizeof(int) * std::max<long long>(nb, 1)) == cudaSuccess &&
+       cudaMallocHost((void**)&b->h_cstage, sizeof(double) * cz::C_NROWS * b->max_cap) == cudaSuccess &&
+       cudaMallocHost((void**)&b->h_cstage_b, sizeof(int) * b->max_cap) == cudaSuccess &&
+       cudaMallocHost((void**)&b->h_pow, sizeof(double) * 2 * P) == cudaSuccess &&
+       cudaMallocHost((void**)&b->h_status, sizeof(uint32_t)) == cudaSuccess;
+  if (!ok) return bail(fail(CZ_ERR_CUDA, "pinned host allocation failed"));
+  cudaStream_t s = b->stream;
+  std::vector<int> bcount(b->counts);
+  if (cudaMemsetAsync(b->body, 0, R * cz::B_NROWS * P, s) != cudaSuccess ||
+      cudaMemsetAsync(b->awake, 0, P, s) != cudaSuccess || cudaMemsetAsync(b->can_sleep, 0, P, s) != cudaSuccess ||
+      cudaMemsetAsync(b->shape, 0xFF, sizeof(int) * P, s) != cudaSuccess ||
+      cudaMemsetAsync(b->d_ccount, 0, sizeof(int) * W, s) != cudaSuccess ||
+      cudaMemsetAsync(b->d_wstatus, 0, sizeof(uint32_t) * W, s) != cudaSuccess ||
+      cudaMemsetAsync(b->d_piters, 0, sizeof(int) * W, s) != cudaSuccess ||
+      cudaMemsetAsync(b->d_viters, 0, sizeof(int) * W, s) != cudaSuccess ||
+      cudaMemsetAsync(b->d_queue, 0, 4 * sizeof(unsigned), s) != cudaSuccess ||
+      cudaMemsetAsync(b->d_status, 0, sizeof(uint32_t), s) != cudaSuccess ||
+      cudaMemsetAsync(b->cbodies, 0xFF, sizeof(int) * C, s) != cudaSuccess ||
+      cudaMemcpyAsync(b->d_bstart, b->bstart.data(), sizeof(int) * W, cudaMemcpyHostToDevice, s) != cudaSuccess ||
+      cudaMemcpyAsync(b->d_bcount, bcount.data(), sizeof(int) * W, cudaMemcpyHostToDevice, s) != cudaSuccess ||
+      cudaMemcpyAsync(b->d_ccap, b->ccap.data(), sizeof(int) * W, cudaMemcpyHostToDevice, s) != cudaSuccess ||
+      cudaMemcpyAsync(b->d_cstart, b->cstart.data(), sizeof(long long) * W, cudaMemcpyHostToDevice, s) !=
+          cudaSuccess ||
+      cudaMemcpyAsync(b->d_order, order.data(), sizeof(int) * W, cudaMemcpyHostToDevice, s) != cudaSuccess ||
+      (nb > 0 &&
+       cudaMemcpyAsync(b->d_h2p, b->h2p.data(), sizeof(int) * nb, cudaMemcpyHostToDevice, s) != cudaSuccess) ||
+      cudaStreamSynchronize(s) != cudaSuccess)
+    return bail(fail(CZ_ERR_CUDA, "device initialisation failed"));
+  b->lin_damp.assign(nb, 0.95);
+  b->ang_damp.assign(nb, 0.95);
+  st = configure(b);
+  if (st != CZ_OK) return bail(st);
+  *out = b;
+  return CZ_OK;
+}
+
+int cz_batch_destroy(cz_batch* b) {
+  if (!b) return fail(CZ_ERR_BAD_ARG, "cz_batch_destroy: null batch");
+  free_batch(b);
+  return CZ_OK;
+}
+
+int cz_set_tuning(cz_batch* b, const cz_tuning* t) {
+  if (!b || !t) return fail(CZ_ERR_BAD_ARG, "cz_set_tuning: null argument");
+  CZ_CUDA(cudaSetDevice(b->device));
+  if (t->narrowphase_threads > 0) {
+    if (t->narrowphase_threads % 32 != 0 || t->narrowphase_threads > 1024)
+      return fail(CZ_ERR_BAD_ARG, "narrowphase_threads must be a multiple of 32, at most 1024");
+    b->np_threads = t->narrowphase_threads;
+  }
+  if (t->resolver_contacts > 0) b->rs_cs = (int)round_up(t->resolver_contacts, 32);
+  if (t->resolver_ctas_per_sm > 0) b->rs_ctas_per_sm = t->resolver_ctas_per_sm;
+  if (t->integrate_threads > 0) {
+    if (t->integrate_threads % 32 != 0 || t->integrate_threads > 256)
+      return fail(CZ_ERR_BAD_ARG, "integrate_threads must be a multiple of 32, at most 256");
+    b->int_threads = t->integrate_threads;
+  }
+  return configure(b);
+}
+
+int cz_get_tuning(cz_batch* b, cz_tuning* t) {
+  if (!b || !t) return fail(CZ_ERR_BAD_ARG, "cz_get_tuning: null argument");
+  t->narrowphase_threads = b->np_threads;
+  t->resolver_contacts = b->rs_cs;
+  t->resolver_ctas_per_sm = b->rs_grid / std::max(b->sm_count, 1);
+  t->integrate_threads = b->int_threads;
+  return CZ_OK;
+}
+
+int cz_upload_bodies(cz_batch* b, const cz_bodies* in) {
+  if (!b || !in) return fail(CZ_ERR_BAD_ARG, "cz_upload_bodies: null argument");
+  if (!in->position || !in->orientation || !in->velocity || !in->rotation || !in->acceleration ||
+      !in->inverse_inertia || !in->inverse_mass || !in->linear_damping || !in->angular_damping || !in->is_awake ||
+      !in->can_sleep || !in->shape || !in->half_size || !in->radius)
+    return fail(CZ_ERR_BAD_ARG, "cz_upload_bodies: missing body field");
+  CZ_CUDA(cudaSetDevice(b->device));
+  const long long n = b->nb;
+  if (n == 0) return CZ_OK;
+  for (long long h = 0; h < n; ++h)
+    if (in->shape[h] != CZ_SHAPE_SPHERE && in->shape[h] != CZ_SHAPE_CUBE)
+      return fail(CZ_ERR_BAD_ARG, "cz_upload_bodies: unknown shape");
+  double* sg = b->h_stage;
+  std::memcpy(sg + cz::SG_POS * n, in->position, sizeof(double) * 3 * n);
+  std::memcpy(sg + cz::SG_Q * n, in->orientation, sizeof(double) * 4 * n);
+  std::memcpy(sg + cz::SG_VEL * n, in->velocity, sizeof(double) * 3 * n);
+  std::memcpy(sg + cz::SG_ROT * n, in->rotation, sizeof(double) * 3 * n);
+  std::memcpy(sg + cz::SG_ACC * n, in->acceleration, sizeof(double) * 3 * n);
+  std::memcpy(sg + cz::SG_IB * n, in->inverse_inertia, sizeof(double) * 9 * n);
+  std::memcpy(sg + cz::SG_INVM * n, in->inverse_mass, sizeof(double) * n);
+  if (in->motion) std::memcpy(sg + cz::SG_MOTION * n, in->motion, sizeof(double) * n);
+  else for (long long h = 0; h < n; ++h) sg[cz::SG_MOTION * n + h] = 0.3 * 2.0;
+  std::memcpy(sg + cz::SG_HALF * n, in->half_size, sizeof(double) * 3 * n);
+  std::memcpy(sg + cz::SG_RAD * n, in->radius, sizeof(double) * n);
+  const int has_iw = in->inverse_inertia_world != nullptr;
+  const int has_lfa = in->last_frame_acceleration != nullptr;
+  if (has_iw) std::memcpy(sg + cz::SG_IW * n, in->inverse_inertia_world, sizeof(double) * 9 * n);
+  if (has_lfa) std::memcpy(sg + cz::SG_LFA * n, in->last_frame_acceleration, sizeof(double) * 3 * n);
+  std::memcpy(b->h_stage_u8, in->is_awake, n);
+  std::memcpy(b->h_stage_u8 + n, in->can_sleep, n);
+  std::memcpy(b->h_stage_i32, in->shape, sizeof(int) * n);
+  b->lin_damp.assign(in->linear_damping, in->linear_damping + n);
+  b->ang_damp.assign(in->angular_damping, in->angular_damping + n);
+  b->pow_dt = std::nan("");
+  CZ_CUDA(cudaMemcpyAsync(b->d_stage, sg, sizeof(double) * cz::SG_NDOUBLES * n, cudaMemcpyHostToDevice, b->stream));
+  CZ_CUDA(cudaMemcpyAsync(b->d_stage_u8, b->h_stage_u8, 2 * n, cudaMemcpyHostToDevice, b->stream));
+  CZ_CUDA(cudaMemcpyAsync(b->d_stage_i32, b->h_stage_i32, sizeof(int) * n, cudaMemcpyHostToDevice, b->stream));
+  CZ_CUDA(b->ops->upload(b->view(), b->d_stage, b->d_stage_u8, b->d_stage_i32, b->d_h2p, (int)n, has_iw, has_lfa,
+                         b->stream));
+  g_launches++;
+  CZ_CUDA(cudaStreamSynchronize(b->stream));
+  return CZ_OK;
+}
+
+int cz_download_bodies(cz_batch* b, cz_bodies* out) {
+  if (!b || !out) return fail(CZ_ERR_BAD_ARG, "cz_download_bodies: null argument");
+  CZ_CUDA(cudaSetDevice(b->device));
+  const long long n = b->nb;
+  if (n == 0) return CZ_OK;
+  CZ_CUDA(b->ops->download(b->view(), b->d_stage, b->d_stage_u8, b->d_stage_i32, b->d_h2p, (int)n, b->stream));
+  g_launches++;
+  CZ_CUDA(cudaMemcpyAsync(b->h_stage, b->d_stage, sizeof(double) * cz::SG_NDOUBLES * n, cudaMemcpyDeviceToHost,
+                          b->stream));
+  CZ_CUDA(cudaMemcpyAsync(b->h_stage_u8, b->d_stage_u8, 2 * n, cudaMemcpyDeviceToHost, b->stream));
+  CZ_CUDA(cudaMemcpyAsync(b->h_stage_i32, b->d_stage_i32, sizeof(int) * n, cudaMemcpyDeviceToHost, b->stream));
+  CZ_CUDA(cudaStreamSynchronize(b->stream));
+  const double* sg = b->h_stage;
+  auto cp = [&](double* dst, int blk, int width) {
+    if (dst) std::memcpy(dst, sg + (long long)blk * n, sizeof(double) * width * n);
+  };
+  cp(out->position, cz::SG_POS, 3);
+  cp(out->orientation, cz::SG_Q, 4);
+  cp(out->velocity, cz::SG_VEL, 3);
+  cp(out->rotation, cz::SG_ROT, 3);
+  cp(out->acceleration, cz::SG_ACC, 3);
+  cp(out->inverse_inertia, cz::SG_IB, 9);
+  cp(out->inverse_mass, cz::SG_INVM, 1);
+  cp(out->motion, cz::SG_MOTION, 1);
+  cp(out->half_size, cz::SG_HALF, 3);
+  cp(out->radius, cz::SG_RAD, 1);
+  cp(out->inverse_inertia_world, cz::SG_IW, 9);
+  cp(out->last_frame_acceleration, cz::SG_LFA, 3);
+  if (out->linear_damping) std::memcpy(out->linear_damping, b->lin_damp.data(), sizeof(double) * n);
+  if (out->angular_damping) std::memcpy(out->angular_damping, b->ang_damp.data(), sizeof(double) * n);
+  if (out->is_awake) std::memcpy(out->is_awake, b->h_stage_u8, n);
+  if (out->can_sleep) std::memcpy(out->can_sleep, b->h_stage_u8 + n, n);
+  if (out->shape) std::memcpy(out->shape, b->h_stage_i32, sizeof(int) * n);
+  return CZ_OK;
+}
+
+int cz_integrate(cz_batch* b, double dt) {
+  if (!b) return fail(CZ_ERR_BAD_ARG, "cz_integrate: null batch");
+  CZ_CUDA(cudaSetDevice(b->device));
+  int st = ensure_pows(b, dt);
+  if (st) return st;
+  if ((st = reset_status(b))) return st;
+  if ((st = launch_integrate(b, dt))) return st;
+  return finish(b);
+}
+
+int cz_narrowphase(cz_batch* b) {
+  if (!b) return fail(CZ_ERR_BAD_ARG, "cz_narrowphase: null batch");
+  CZ_CUDA(cudaSetDevice(b->device));
+  int st = reset_status(b);
+  if (st) return st;
+  if ((st = launch_narrowphase(b))) return st;
+  return finish(b);
+}
+
+int cz_resolve(cz_batch* b, double dt) {
+  if (!b) return fail(CZ_ERR_BAD_ARG, "cz_resolve: null batch");
+  CZ_CUDA(cudaSetDevice(b->device));
+  int st = reset_status(b);
+  if (st) return st;
+  if ((st = launch_resolve(b, dt))) return st;
+  return finish(b);
+}
+
+int cz_step(cz_batch* b, int32_t nsteps, double dt) {
+  if (!b || nsteps < 0) return fail(CZ_ERR_BAD_ARG, "cz_step: bad argument");
+  if (nsteps == 0) return CZ_OK;
+  CZ_CUDA(cudaSetDevice(b->device));
+  int st = ensure_pows(b, dt);
+  if (st) return st;
+  if ((st = reset_status(b))) return st;
+  auto key = std::make_pair((int)nsteps, dt);
+  auto it = b->graphs.find(key);
+  if (it == b->graphs.end()) {
+    // capture the rollout once: per step, integrate -> narrowphase -> resolve
+    CZ_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+    const long long before = g_launches.load();
+    int cst = CZ_OK;
+    for (int s = 0; s < nsteps && cst == CZ_OK; ++s) {
+      cst = launch_integrate(b, dt);
+      if (!cst) cst = launch_narrowphase(b);
+      if (!cst) cst = launch_resolve(b, dt);
+    }
+    g_launches.store(before);  // captured launches are counted when the graph runs
+    cudaGraph_t graph = nullptr;
+    cudaError_t e = cudaStreamEndCapture(b->stream, &graph);
+    if (cst != CZ_OK) {
+      if (graph) cudaGraphDestroy(graph);
+      return cst;
+    }
+    if (e != cudaSuccess) return fail(CZ_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+    cudaGraphExec_t exec = nullptr;
+    e = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return fail(CZ_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+    it = b->graphs.emplace(key, exec).first;
+  }
+  CZ_CUDA(cudaGraphLaunch(it->second, b->stream));
+  g_launches += 3LL * nsteps;
+  return finish(b);
+}
+
+int cz_contact_counts(cz_batch* b, int32_t* counts) {
+  if (!b || !counts) return fail(CZ_ERR_BAD_ARG, "cz_contact_counts: null argument");
+  CZ_CUDA(cudaSetDevice(b->device));
+  CZ_CUDA(cudaMemcpyAsync(counts, b->d_ccount, sizeof(int) * b->num_worlds, cudaMemcpyDeviceToHost, b->stream));
+  CZ_CUDA(cudaStreamSynchronize(b->stream));
+  return CZ_OK;
+}
+
+int cz_download_contacts(cz_batch* b, int32_t world, cz_contact* out, int32_t capacity, int32_t* count) {
+  if (!b || world < 0 || world >= b->num_worlds || (capacity > 0 && !out))
+    return fail(CZ_ERR_BAD_ARG, "cz_download_contacts: bad argument");
+  CZ_CUDA(cudaSetDevice(b->device));
+  int n = 0;
+  CZ_CUDA(cudaMemcpyAsync(&n, b->d_ccount + world, sizeof(int), cudaMemcpyDeviceToHost, b->stream));
+  CZ_CUDA(cudaStreamSynchronize(b->stream));
+  if (count) *count = n;
+  int m = std::min(n, b->ccap[world]);
+  m = std::min(m, std::max(capacity, 0));
+  if (m <= 0) return n > b->ccap[world] ? fail(CZ_ERR_CAPACITY, "world exceeded its contact capacity") : CZ_OK;
+  CZ_CUDA(b->ops->contacts_out(b->view(), b->cstart[world], m, b->d_cstage, b->d_cstage_b, b->stream));
+  g_launches++;
+  CZ_CUDA(cudaMemcpyAsync(b->h_cstage, b->d_cstage, sizeof(double) * cz::C_NROWS * m, cudaMemcpyDeviceToHost,
+                          b->stream));
+  CZ_CUDA(cudaMemcpyAsync(b->h_cstage_b, b->d_cstage_b, sizeof(int) * m, cudaMemcpyDeviceToHost, b->stream));
+  CZ_CUDA(cudaStreamSynchronize(b->stream));
+  for (int k = 0; k < m; ++k) {
+    const double* c = b->h_cstage + (long long)k * cz::C_NROWS;
+    cz_contact& o = out[k];
+    o.body[0] = cz::body0_of(b->h_cstage_b[k]);
+    o.body[1] = cz::body1_of(b->h_cstage_b[k]);
+    o.point[0] = c[cz::C_PX]; o.point[1] = c[cz::C_PY]; o.point[2] = c[cz::C_PZ];
+    o.normal[0] = c[cz::C_NX]; o.normal[1] = c[cz::C_NY]; o.normal[2] = c[cz::C_NZ];
+    o.penetration = c[cz::C_PEN];
+    o.friction = c[cz::C_FRIC];
+    o.restitution = c[cz::C_REST];
+  }
+  if (n > b->ccap[world]) return fail(CZ_ERR_CAPACITY, "world exceeded its contact capacity");
+  return CZ_OK;
+}
+
+int cz_world_stats(cz_batch* b, int32_t* pos_it, int32_t* vel_it, uint32_t* status) {
+  if (!b) return fail(CZ_ERR_BAD_ARG, "cz_world_stats: null batch");
+  CZ_CUDA(cudaSetDevice(b->device));
+  const size_t W = b->num_worlds;
+  if (pos_it) CZ_CUDA(cudaMemcpyAsync(pos_it, b->d_piters, sizeof(int) * W, cudaMemcpyDeviceToHost, b->stream));
+  if (vel_it) CZ_CUDA(cudaMemcpyAsync(vel_it, b->d_viters, sizeof(int) * W, cudaMemcpyDeviceToHost, b->stream));
+  if (status) CZ_CUDA(cudaMemcpyAsync(status, b->d_wstatus, sizeof(uint32_t) * W, cudaMemcpyDeviceToHost, b->stream));
+  CZ_CUDA(cudaStreamSynchronize(b->stream));
+  return CZ_OK;
+}
+
+int cz_resolve_contacts(cz_batch* b, int32_t max_iterations, cz_contact* contacts, int32_t ncontacts,
+                        double duration, cz_bodies* bodies) {
+  if (!b || !bodies || ncontacts < 0 || (ncontacts > 0 && !contacts))
+    return fail(CZ_ERR_BAD_ARG, "cz_resolve_contacts: bad argument");
+  if (b->num_worlds != 1) return fail(CZ_ERR_BAD_ARG, "cz_resolve_contacts: the batch must hold one world");
+  if (ncontacts > b->ccap[0]) return fail(CZ_ERR_CAPACITY, "cz_resolve_contacts: more contacts than capacity");
+  // ResolveContacts' own guards (contact.go:210-212): nothing changes
+  if (duration <= 0.0 || ncontacts == 0) return CZ_OK;
+  const int n = b->counts[0];
+  for (int k = 0; k < ncontacts; ++k) {
+    const int b0 = contacts[k].body[0], b1 = contacts[k].body[1];
+    if (b0 < -1 || b0 >= n || b1 < -1 || b1 >= n || (b0 < 0 && b1 < 0))
+      return fail(CZ_ERR_BAD_ARG, "cz_resolve_contacts: contact body index out of range");
+  }
+  int st = cz_upload_bodies(b, bodies);
+  if (st) return st;
+  CZ_CUDA(cudaSetDevice(b->device));
+  for (int k = 0; k < ncontacts; ++k) {
+    double* c = b->h_cstage + (long long)k * cz::C_NROWS;
+    const cz_contact& s = contacts[k];
+    c[cz::C_PX] = s.point[0]; c[cz::C_PY] = s.point[1]; c[cz::C_PZ] = s.point[2];
+    c[cz::C_NX] = s.normal[0]; c[cz::C_NY] = s.normal[1]; c[cz::C_NZ] = s.normal[2];
+    c[cz::C_PEN] = s.penetration;
+    c[cz::C_FRIC] = s.friction;
+    c[cz::C_REST] = s.restitution;
+    b->h_cstage_b[k] = cz::pack_bodies(s.body[0], s.body[1]);
+  }
+  CZ_CUDA(cudaMemcpyAsync(b->d_cstage, b->h_cstage, sizeof(double) * cz::C_NROWS * ncontacts, cudaMemcpyHostToDevice,
+                          b->stream));
+  CZ_CUDA(cudaMemcpyAsync(b->d_cstage_b, b->h_cstage_b, sizeof(int) * ncontacts, cudaMemcpyHostToDevice, b->stream));
+  CZ_CUDA(b->ops->contacts_in(b->view(), b->cstart[0], ncontacts, b->d_cstage, b->d_cstage_b, b->stream));
+  g_launches++;
+  CZ_CUDA(cudaMemcpyAsync(b->d_ccount, &ncontacts, sizeof(int), cudaMemcpyHostToDevice, b->stream));
+  if ((st = reset_status(b))) return st;
+  cz::HostView v = b->view();
+  v.max_iterations = std::max(max_iterations, 0);
+  v.contact_writeback = 1;
+  if ((st = launch_resolve(b, duration, &v))) return st;
+  st = finish(b);
+  if (st != CZ_OK && st != CZ_ERR_FRICTIONLESS) return st;
+  const int st2 = cz_download_bodies(b, bodies);
+  if (st2) return st2;
+  // write the resolved contacts back (penetration, swapped bodies/normal)
+  CZ_CUDA(b->ops->contacts_out(b->view(), b->cstart[0], ncontacts, b->d_cstage, b->d_cstage_b, b->stream));
+  g_launches++;
+  CZ_CUDA(cudaMemcpyAsync(b->h_cstage, b->d_cstage, sizeof(double) * cz::C_NROWS * ncontacts, cudaMemcpyDeviceToHost,
+                          b->stream));
+  CZ_CUDA(cudaMemcpyAsync(b->h_cstage_b, b->d_cstage_b, sizeof(int) * ncontacts, cudaMemcpyDeviceToHost, b->stream));
+  CZ_CUDA(cudaStreamSynchronize(b->stream));
+  for (int k = 0; k < ncontacts; ++k) {
+    const double* c = b->h_cstage + (long long)k * cz::C_NROWS;
+    contacts[k].body[0] = cz::body0_of(b->h_cstage_b[k]);
+    contacts[k].body[1] = cz::body1_of(b->h_cstage_b[k]);
+    contacts[k].normal[0] = c[cz::C_NX];
+    contacts[k].normal[1] = c[cz::C_NY];
+    contacts[k].normal[2] = c[cz::C_NZ];
+    contacts[k].penetration = c[cz::C_PEN];
+  }
+  return st;
+}
+
+}  // extern "C"

@@ -1,0 +1,236 @@
+// Kernel instantiation and launch wrappers for one form; included by
+// cz_fp64.cu / cz_fp32.cu with CZ_R, CZ_W and CZ_FORM_NAME defined.
+#pragma once
+#include "cz_forms.h"
+#include "cz_kernels.cuh"
+
+namespace cz {
+namespace CZ_FORM_NS {
+
+using R = CZ_R;
+using W = CZ_W;
+
+static BatchView<R> view_of(const HostView& h) {
+  BatchView<R> v;
+  v.body = static_cast<R*>(h.body);
+  v.awake = h.awake;
+  v.can_sleep = h.can_sleep;
+  v.shape = h.shape;
+  v.nb_pad = h.nb_pad;
+  v.num_worlds = h.num_worlds;
+  v.max_bodies = h.max_bodies;
+  v.body_start = h.body_start;
+  v.body_count = h.body_count;
+  v.contact_start = h.contact_start;
+  v.contact_cap = h.contact_cap;
+  v.contact_count = h.contact_count;
+  v.world_status = h.world_status;
+  v.pos_iters = h.pos_iters;
+  v.vel_iters = h.vel_iters;
+  v.contact = static_cast<R*>(h.contact);
+  v.contact_bodies = h.contact_bodies;
+  v.work = static_cast<R*>(h.work);
+  v.work_bodies = h.work_bodies;
+  v.nc_total = h.nc_total;
+  v.order = h.order;
+  v.queue = h.queue;
+  v.status = h.status;
+  v.plane_nx = (R)h.plane[0];
+  v.plane_ny = (R)h.plane[1];
+  v.plane_nz = (R)h.plane[2];
+  v.plane_offset = (R)h.plane[3];
+  v.iter_mult = h.iter_mult;
+  v.max_iterations = h.max_iterations;
+  v.contact_writeback = h.contact_writeback;
+  return v;
+}
+
+// Host body data (staged AoS doubles) -> device rows, then
+// CalculateDerivedData where no world inertia was given.
+__global__ void k_upload(BatchView<R> v, const double* __restrict__ sg, const uint8_t* __restrict__ u8,
+                         const int* __restrict__ i32, const int* __restrict__ h2p, int nb, int has_iw, int has_lfa) {
+  const int h = blockIdx.x * blockDim.x + threadIdx.x;
+  if (h >= nb) return;
+  const long long p = h2p[h];
+  const long long S = v.nb_pad;
+  const long long n = nb;
+  R* b = v.body + p;
+  for (int k = 0; k < 3; ++k) {
+    b[(B_PX + k) * S] = (R)sg[SG_POS * n + 3 * h + k];
+    b[(B_VX + k) * S] = (R)sg[SG_VEL * n + 3 * h + k];
+    b[(B_RX + k) * S] = (R)sg[SG_ROT * n + 3 * h + k];
+    b[(B_AX + k) * S] = (R)sg[SG_ACC * n + 3 * h + k];
+    b[(B_HX + k) * S] = (R)sg[SG_HALF * n + 3 * h + k];
+    b[(B_LX + k) * S] = has_lfa ? (R)sg[SG_LFA * n + 3 * h + k] : (R)0;
+  }
+  q4<R> q{(R)sg[SG_Q * n + 4 * h], (R)sg[SG_Q * n + 4 * h + 1], (R)sg[SG_Q * n + 4 * h + 2],
+          (R)sg[SG_Q * n + 4 * h + 3]};
+  m3<R> ib;
+  for (int k = 0; k < 9; ++k) ib.m[k] = (R)sg[SG_IB * n + 9 * h + k];
+  m3<R> iw;
+  if (has_iw) {
+    for (int k = 0; k < 9; ++k) iw.m[k] = (R)sg[SG_IW * n + 9 * h + k];
+  } else {
+    // RigidBody.CalculateDerivedData, rigidbody.go:268-272
+    q4<W> qw = cvtq<W>(q);
+    qnormalize(qw);
+    q = cvtq<R>(qw);
+    R rm[9];
+    rotation_of(q, rm);
+    iw = world_inertia(rm, ib);
+  }
+  b[B_QW * S] = q.w; b[B_QX * S] = q.x; b[B_QY * S] = q.y; b[B_QZ * S] = q.z;
+  for (int k = 0; k < 9; ++k) {
+    b[(B_IB0 + k) * S] = ib.m[k];
+    b[(B_IW0 + k) * S] = iw.m[k];
+  }
+  b[B_INVM * S] = (R)sg[SG_INVM * n + h];
+  b[B_MOTION * S] = (R)sg[SG_MOTION * n + h];
+  b[B_RAD * S] = (R)sg[SG_RAD * n + h];
+  v.awake[p] = u8[h];
+  v.can_sleep[p] = u8[n + h];
+  v.shape[p] = i32[h];
+}
+
+__global__ void k_download(BatchView<R> v, double* __restrict__ sg, uint8_t* __restrict__ u8, int* __restrict__ i32,
+                           const int* __restrict__ h2p, int nb) {
+  const int h = blockIdx.x * blockDim.x + threadIdx.x;
+  if (h >= nb) return;
+  const long long p = h2p[h];
+  const long long S = v.nb_pad;
+  const long long n = nb;
+  const R* b = v.body + p;
+  for (int k = 0; k < 3; ++k) {
+    sg[SG_POS * n + 3 * h + k] = (double)b[(B_PX + k) * S];
+    sg[SG_VEL * n + 3 * h + k] = (double)b[(B_VX + k) * S];
+    sg[SG_ROT * n + 3 * h + k] = (double)b[(B_RX + k) * S];
+    sg[SG_ACC * n + 3 * h + k] = (double)b[(B_AX + k) * S];
+    sg[SG_HALF * n + 3 * h + k] = (double)b[(B_HX + k) * S];
+    sg[SG_LFA * n + 3 * h + k] = (double)b[(B_LX + k) * S];
+  }
+  sg[SG_Q * n + 4 * h + 0] = (double)b[B_QW * S];
+  sg[SG_Q * n + 4 * h + 1] = (double)b[B_QX * S];
+  sg[SG_Q * n + 4 * h + 2] = (double)b[B_QY * S];
+  sg[SG_Q * n + 4 * h + 3] = (double)b[B_QZ * S];
+  for (int k = 0; k < 9; ++k) {
+    sg[SG_IB * n + 9 * h + k] = (double)b[(B_IB0 + k) * S];
+    sg[SG_IW * n + 9 * h + k] = (double)b[(B_IW0 + k) * S];
+  }
+  sg[SG_INVM * n + h] = (double)b[B_INVM * S];
+  sg[SG_MOTION * n + h] = (double)b[B_MOTION * S];
+  sg[SG_RAD * n + h] = (double)b[B_RAD * S];
+  u8[h] = v.awake[p];
+  u8[n + h] = v.can_sleep[p];
+  i32[h] = v.shape[p];
+}
+
+__global__ void k_contacts_out(BatchView<R> v, long long start, int count, double* __restrict__ sg,
+                               int* __restrict__ bodies) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= count) return;
+  const long long S = v.nc_total;
+  const R* c = v.contact + start + k;
+  for (int f = 0; f < C_NROWS; ++f) sg[(long long)k * C_NROWS + f] = (double)c[f * S];
+  bodies[k] = v.contact_bodies[start + k];
+}
+
+__global__ void k_contacts_in(BatchView<R> v, long long start, int count, const double* __restrict__ sg,
+                              const int* __restrict__ bodies) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= count) return;
+  const long long S = v.nc_total;
+  R* c = v.contact + start + k;
+  for (int f = 0; f < C_NROWS; ++f) c[f * S] = (R)sg[(long long)k * C_NROWS + f];
+  v.contact_bodies[start + k] = bodies[k];
+}
+
+__global__ void k_set_rows(BatchView<R> v, int row, int nrows, const double* __restrict__ src) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long total = (long long)nrows * v.nb_pad;
+  if (i >= total) return;
+  v.body[(long long)row * v.nb_pad + i] = (R)src[i];
+}
+
+static size_t np_smem(int nbs) { return np_smem_bytes<R>(nbs); }
+static size_t rs_smem(int nbs, int cs) { return rs_smem_bytes<R, W>(nbs, cs); }
+
+static cudaError_t prepare(size_t np, size_t rs) {
+  cudaError_t e = cudaFuncSetAttribute(k_narrowphase<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)np);
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(k_resolve<R, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rs);
+}
+
+static cudaError_t integrate(const HostView& h, double dt, double bias, int threads, cudaStream_t s) {
+  const long long nb = h.nb_pad;
+  const int grid = (int)((nb + threads - 1) / threads);
+  k_integrate<R, W><<<grid, threads, 0, s>>>(view_of(h), (R)dt, (R)bias);
+  return cudaGetLastError();
+}
+
+static cudaError_t narrowphase(const HostView& h, int nbs, int threads, int grid, size_t smem, cudaStream_t s) {
+  k_narrowphase<R><<<grid, threads, smem, s>>>(view_of(h), nbs);
+  return cudaGetLastError();
+}
+
+static cudaError_t resolve(const HostView& h, int nbs, int cs, int grid, size_t smem, double dt, cudaStream_t s) {
+  k_resolve<R, W><<<grid, 32, smem, s>>>(view_of(h), nbs, cs, (R)dt);
+  return cudaGetLastError();
+}
+
+static cudaError_t upload(const HostView& h, const double* sg, const uint8_t* u8, const int* i32, const int* h2p,
+                          int nb, int has_iw, int has_lfa, cudaStream_t s) {
+  if (nb <= 0) return cudaSuccess;
+  k_upload<<<(nb + 255) / 256, 256, 0, s>>>(view_of(h), sg, u8, i32, h2p, nb, has_iw, has_lfa);
+  return cudaGetLastError();
+}
+
+static cudaError_t download(const HostView& h, double* sg, uint8_t* u8, int* i32, const int* h2p, int nb,
+                            cudaStream_t s) {
+  if (nb <= 0) return cudaSuccess;
+  k_download<<<(nb + 255) / 256, 256, 0, s>>>(view_of(h), sg, u8, i32, h2p, nb);
+  return cudaGetLastError();
+}
+
+static cudaError_t occupancy(int* npb, int np_threads, size_t nps, int* rsb, size_t rss) {
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(npb, k_narrowphase<R>, np_threads, nps);
+  if (e != cudaSuccess) return e;
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(rsb, k_resolve<R, W>, 32, rss);
+}
+
+static cudaError_t contacts_out(const HostView& h, long long start, int count, double* sg, int* bodies,
+                                cudaStream_t s) {
+  if (count <= 0) return cudaSuccess;
+  k_contacts_out<<<(count + 127) / 128, 128, 0, s>>>(view_of(h), start, count, sg, bodies);
+  return cudaGetLastError();
+}
+
+static cudaError_t contacts_in(const HostView& h, long long start, int count, const double* sg, const int* bodies,
+                               cudaStream_t s) {
+  if (count <= 0) return cudaSuccess;
+  k_contacts_in<<<(count + 127) / 128, 128, 0, s>>>(view_of(h), start, count, sg, bodies);
+  return cudaGetLastError();
+}
+
+static cudaError_t set_rows(const HostView& h, int row, int nrows, const double* src, cudaStream_t s) {
+  const long long total = (long long)nrows * h.nb_pad;
+  k_set_rows<<<(int)((total + 255) / 256), 256, 0, s>>>(view_of(h), row, nrows, src);
+  return cudaGetLastError();
+}
+
+}  // namespace CZ_FORM_NS
+
+const FormOps CZ_FORM_OBJ = {sizeof(CZ_R),
+                             CZ_FORM_NS::np_smem,
+                             CZ_FORM_NS::rs_smem,
+                             CZ_FORM_NS::prepare,
+                             CZ_FORM_NS::integrate,
+                             CZ_FORM_NS::narrowphase,
+                             CZ_FORM_NS::resolve,
+                             CZ_FORM_NS::upload,
+                             CZ_FORM_NS::download,
+                             CZ_FORM_NS::occupancy,
+                             CZ_FORM_NS::contacts_out,
+                             CZ_FORM_NS::contacts_in,
+                             CZ_FORM_NS::set_rows};
+
+}  // namespace cz

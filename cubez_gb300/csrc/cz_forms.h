@@ -1,0 +1,72 @@
+// Host-side interface between the C ABI (cz_api.cu) and the per-form kernel
+// instantiations (cz_fp64.cu, cz_fp32.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+
+namespace cz {
+
+// Type-erased device view; each form turns it into BatchView<R>.
+struct HostView {
+  void* body;
+  uint8_t* awake;
+  uint8_t* can_sleep;
+  int32_t* shape;
+  long long nb_pad;
+  int num_worlds;
+  int max_bodies;
+  const int* body_start;
+  const int* body_count;
+  const long long* contact_start;
+  const int* contact_cap;
+  int* contact_count;
+  uint32_t* world_status;
+  int* pos_iters;
+  int* vel_iters;
+  void* contact;
+  int* contact_bodies;
+  void* work;
+  int* work_bodies;
+  long long nc_total;
+  const int* order;
+  unsigned* queue;
+  uint32_t* status;
+  double plane[4];
+  int iter_mult;
+  int max_iterations;
+  int contact_writeback;
+};
+
+// Staging layout of host body data on the device (doubles, field blocks of n):
+enum StageBlock : int {
+  SG_POS = 0, SG_Q = 3, SG_VEL = 7, SG_ROT = 10, SG_ACC = 13, SG_IB = 16, SG_INVM = 25, SG_MOTION = 26,
+  SG_HALF = 27, SG_RAD = 30, SG_IW = 31, SG_LFA = 40, SG_NDOUBLES = 43
+};
+
+struct FormOps {
+  size_t real_size;
+  size_t (*np_smem)(int nbs);
+  size_t (*rs_smem)(int nbs, int cs);
+  cudaError_t (*prepare)(size_t np_smem, size_t rs_smem);  // function attributes
+  cudaError_t (*integrate)(const HostView& v, double dt, double sleep_bias, int threads, cudaStream_t s);
+  cudaError_t (*narrowphase)(const HostView& v, int nbs, int threads, int grid, size_t smem, cudaStream_t s);
+  cudaError_t (*resolve)(const HostView& v, int nbs, int cs, int grid, size_t smem, double dt, cudaStream_t s);
+  cudaError_t (*upload)(const HostView& v, const double* stage, const uint8_t* u8, const int* i32, const int* h2p,
+                        int nb, int has_iw, int has_lfa, cudaStream_t s);
+  cudaError_t (*download)(const HostView& v, double* stage, uint8_t* u8, int* i32, const int* h2p, int nb,
+                          cudaStream_t s);
+  cudaError_t (*occupancy)(int* np_blocks, int np_threads, size_t np_smem, int* rs_blocks, size_t rs_smem);
+  // contacts: device rows <-> AoS doubles staging (10 doubles + 2 ints per contact)
+  cudaError_t (*contacts_out)(const HostView& v, long long start, int count, double* stage, int* bodies,
+                              cudaStream_t s);
+  cudaError_t (*contacts_in)(const HostView& v, long long start, int count, const double* stage, const int* bodies,
+                             cudaStream_t s);
+  cudaError_t (*set_rows)(const HostView& v, int row, int nrows, const double* src, cudaStream_t s);
+};
+
+extern const FormOps kFormFP64;
+extern const FormOps kFormFP32;
+
+}  // namespace cz

@@ -1,0 +1,99 @@
+// Device layout of a batch of independent worlds (structure of arrays).
+//
+// Bodies: one row per field, each row `nb_pad` long; world w owns rows
+// [body_start[w], body_start[w] + body_count[w]) with body_start a multiple of
+// 4, so that every world's slice of a row starts on a 16-byte (float) or
+// 32-byte (double) boundary and can be staged with a bulk copy.
+// Contacts: one row per field, each `nc_total` long; world w owns
+// [contact_start[w], contact_start[w] + contact_cap[w]).
+#pragma once
+#include <cstdint>
+
+namespace cz {
+
+enum BodyRow : int {
+  B_PX, B_PY, B_PZ,                                      // RigidBody.Position
+  B_QW, B_QX, B_QY, B_QZ,                                // RigidBody.Orientation
+  B_HX, B_HY, B_HZ, B_RAD,                               // CollisionCube.HalfSize / CollisionSphere.Radius
+  B_VX, B_VY, B_VZ,                                      // Velocity
+  B_RX, B_RY, B_RZ,                                      // Rotation (angular velocity)
+  B_AX, B_AY, B_AZ,                                      // Acceleration
+  B_LX, B_LY, B_LZ,                                      // lastFrameAccelleration
+  B_IB0, B_IB1, B_IB2, B_IB3, B_IB4, B_IB5, B_IB6, B_IB7, B_IB8,  // InverseInertiaTensor (body)
+  B_IW0, B_IW1, B_IW2, B_IW3, B_IW4, B_IW5, B_IW6, B_IW7, B_IW8,  // inverseInertiaTensorWorld
+  B_INVM,                                                // inverseMass
+  B_LINPOW, B_ANGPOW,                                    // pow(LinearDamping, dt), pow(AngularDamping, dt)
+  B_MOTION,                                              // motion
+  B_NROWS
+};
+
+// Narrowphase output (Contact fields set by the colliders).
+enum ContactRow : int { C_PX, C_PY, C_PZ, C_NX, C_NY, C_NZ, C_PEN, C_FRIC, C_REST, C_NROWS };
+
+// Resolver working set (Contact's private fields, contact.go:38-50).
+enum WorkRow : int {
+  W_PEN, W_DDV,
+  W_NX, W_NY, W_NZ,
+  W_TYX, W_TYY, W_TYZ,
+  W_TZX, W_TZY, W_TZZ,
+  W_R0X, W_R0Y, W_R0Z,
+  W_R1X, W_R1Y, W_R1Z,
+  W_CVX, W_CVY, W_CVZ,
+  W_FRIC, W_REST,
+  W_NROWS
+};
+
+// World status bits (also OR-ed into the batch status word).
+enum : uint32_t {
+  ST_NONFINITE = 1u,        // box-box test reached with no accepted axis (non-finite state)
+  ST_FRICTIONLESS_NIL = 2u, // frictionless impulse on a single-body contact (the reference panics)
+  ST_CAPACITY = 4u,         // more contacts than the world's capacity
+  ST_TIMEOUT = 8u,          // a bounded wait gave up
+  ST_BODY_LIMIT = 16u,      // world larger than the kernel's shared-memory tile
+};
+
+// packed body pair of a contact: low 16 bits body 0, high 16 bits body 1
+// (0xFFFF = nil).  World-local indices, so a world holds at most 65535 bodies.
+__host__ __device__ __forceinline__ int pack_bodies(int b0, int b1) {
+  return (int)(((unsigned)(b0 & 0xFFFF)) | ((unsigned)(b1 & 0xFFFF) << 16));
+}
+__host__ __device__ __forceinline__ int body0_of(int p) {
+  int b = p & 0xFFFF;
+  return b == 0xFFFF ? -1 : b;
+}
+__host__ __device__ __forceinline__ int body1_of(int p) {
+  int b = (int)(((unsigned)p) >> 16);
+  return b == 0xFFFF ? -1 : b;
+}
+
+template <class R> struct BatchView {
+  R* body;              // [B_NROWS][nb_pad]
+  uint8_t* awake;       // [nb_pad]
+  uint8_t* can_sleep;   // [nb_pad]
+  int32_t* shape;       // [nb_pad] 0 sphere, 1 cube, -1 padding
+  long long nb_pad;
+  int num_worlds;
+  int max_bodies;       // largest world
+  const int* body_start;
+  const int* body_count;
+  const long long* contact_start;
+  const int* contact_cap;
+  int* contact_count;   // [num_worlds] narrowphase output
+  uint32_t* world_status;
+  int* pos_iters;
+  int* vel_iters;
+  R* contact;           // [C_NROWS][nc_total]
+  int* contact_bodies;  // [nc_total]
+  R* work;              // [W_NROWS][nc_total]
+  int* work_bodies;     // [nc_total]
+  long long nc_total;
+  const int* order;     // world queue: worlds in decreasing cost
+  unsigned* queue;      // [0] narrowphase, [1] resolver, [2..3] spare
+  uint32_t* status;     // batch status word
+  R plane_nx, plane_ny, plane_nz, plane_offset;
+  int iter_mult;        // ResolveContacts(len(contacts) * iter_mult)
+  int max_iterations;   // >= 0 overrides len(contacts) * iter_mult
+  int contact_writeback; // copy the resolved contacts back to the contact rows
+};
+
+}  // namespace cz

@@ -1,0 +1,168 @@
+/*
+ * cubez_gpu.h - C ABI of the GB300 (sm_103a) rigid-body step.
+ *
+ * This is the boundary a cgo binding of cubez binds: plain pointers, sizes and
+ * int status codes, no CUDA or C++ types.  Bodies and contacts live on the
+ * device in structure-of-arrays form inside a batch handle; the host passes
+ * and receives array-of-structures doubles laid out like cubez's value types
+ * (m.Vector3 = 3 doubles, m.Quat = (w,x,y,z), m.Matrix3 = 9 doubles
+ * column-major).  Worlds in a batch are independent: contacts of one world
+ * never touch bodies of another (contact.go:204-207 recommends exactly this
+ * split for ResolveContacts).
+ *
+ * Reference interfaces replaced (tbogdala/cubez):
+ *   RigidBody fields/methods ........ rigidbody.go:23-272
+ *   RigidBody.Integrate ............. rigidbody.go:213-259  -> cz_integrate / cz_step
+ *   RigidBody.CalculateDerivedData .. rigidbody.go:268-272  -> cz_upload_bodies
+ *   Collider.CheckAgainst{HalfSpace,Sphere,Cube}, CheckForCollisions
+ *                                     colliders.go:15-23, 178-710, 720-747
+ *                                                           -> cz_narrowphase / cz_step
+ *   the per-frame loop of examples/cubedrop.go:29-75      -> cz_step
+ *   ResolveContacts ................. contact.go:208-222    -> cz_resolve / cz_resolve_contacts
+ *   Contact (exported fields) ....... contact.go:17-36      -> cz_contact
+ *
+ * Every function returns a cz_status.  Nothing traps on the device: conditions
+ * under which the Go reference panics (non-finite box transforms, a
+ * frictionless single-body contact) are reported as status bits.
+ */
+#ifndef CUBEZ_GPU_H
+#define CUBEZ_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum cz_status {
+  CZ_OK = 0,
+  CZ_ERR_BAD_ARG = 1,      /* invalid handle, size or pointer */
+  CZ_ERR_CUDA = 2,         /* a CUDA call failed; see cz_last_error() */
+  CZ_ERR_NO_DEVICE = 3,    /* no CUDA device */
+  CZ_ERR_NONFINITE = 4,    /* non-finite box transform met in the box-box test (the reference panics) */
+  CZ_ERR_CAPACITY = 5,     /* a world produced more contacts than its capacity */
+  CZ_ERR_TIMEOUT = 6,      /* a bounded device wait gave up */
+  CZ_ERR_FRICTIONLESS = 7, /* frictionless impulse on a single-body contact (contact.go:512 dereferences nil) */
+  CZ_ERR_BODY_LIMIT = 8,   /* a world has more bodies than the kernels' tile; raise max_bodies */
+} cz_status;
+
+typedef enum cz_form {
+  CZ_FORM_FP64 = 0, /* plain form: every operation in float64, as the reference */
+  CZ_FORM_FP32 = 1, /* precision form: float32, with float64 for quaternion renormalisation,
+                       the positions/orientations accumulated across adjustPositions and the
+                       contact-frame 3x3 inversion of the friction impulse */
+} cz_form;
+
+typedef enum cz_shape { CZ_SHAPE_SPHERE = 0, CZ_SHAPE_CUBE = 1 } cz_shape;
+
+typedef struct cz_batch cz_batch; /* opaque */
+
+/* Batch description (cz_batch_create). */
+typedef struct cz_batch_desc {
+  int32_t form;                 /* cz_form */
+  int32_t num_worlds;
+  const int32_t* body_counts;   /* [num_worlds] bodies per world (world-local index < 65535) */
+  int32_t contact_capacity;     /* per world; 0 = worst case 8n + n(n-1) capped at 64n */
+  double plane[4];              /* the ground CollisionPlane: normal xyz, offset (colliders.go:29-35) */
+  int32_t iteration_multiplier; /* ResolveContacts(len(contacts) * k, ...) as examples/cubedrop.go:73; 0 = 4 */
+  int32_t max_iterations;       /* > 0: a fixed maxIterations instead of len(contacts) * k */
+  int32_t device;               /* CUDA device ordinal */
+} cz_batch_desc;
+
+/* Host array-of-structures body data, world-major (bodies of world 0 first).
+ * Fields mirror RigidBody (rigidbody.go:23-101) and the collider shapes
+ * (colliders.go:37-71).  On download, NULL pointers are skipped. */
+typedef struct cz_bodies {
+  double* position;                /* [n][3]  RigidBody.Position */
+  double* orientation;             /* [n][4]  RigidBody.Orientation (w,x,y,z) */
+  double* velocity;                /* [n][3]  RigidBody.Velocity */
+  double* rotation;                /* [n][3]  RigidBody.Rotation (angular velocity) */
+  double* acceleration;            /* [n][3]  RigidBody.Acceleration */
+  double* inverse_inertia;         /* [n][9]  RigidBody.InverseInertiaTensor (body space) */
+  double* inverse_mass;            /* [n]     1/mass (SetMass) or 0 (SetInfiniteMass) */
+  double* linear_damping;          /* [n]     RigidBody.LinearDamping */
+  double* angular_damping;         /* [n]     RigidBody.AngularDamping */
+  double* motion;                  /* [n]     sleep motion average */
+  uint8_t* is_awake;               /* [n]     RigidBody.IsAwake */
+  uint8_t* can_sleep;              /* [n]     RigidBody.CanSleep */
+  int32_t* shape;                  /* [n]     cz_shape */
+  double* half_size;               /* [n][3]  CollisionCube.HalfSize */
+  double* radius;                  /* [n]     CollisionSphere.Radius */
+  double* inverse_inertia_world;   /* [n][9]  derived; upload: NULL = CalculateDerivedData */
+  double* last_frame_acceleration; /* [n][3]  derived; upload: NULL = zero */
+} cz_bodies;
+
+/* One contact, the exported fields of Contact (contact.go:17-36).  Bodies are
+ * world-local indices, -1 for nil. */
+typedef struct cz_contact {
+  int32_t body[2];
+  double friction;
+  double restitution;
+  double point[3];
+  double normal[3];
+  double penetration;
+} cz_contact;
+
+/* Create / destroy a batch of worlds on one GPU.  Allocates all device memory
+ * up front; no later call allocates. */
+int cz_batch_create(const cz_batch_desc* desc, cz_batch** out);
+int cz_batch_destroy(cz_batch* batch);
+
+/* Copy bodies in (and run RigidBody.CalculateDerivedData + the colliders'
+ * CalculateDerivedData, rigidbody.go:268-272, colliders.go:173-176/302-304),
+ * or copy the current state out.  Blocking. */
+int cz_upload_bodies(cz_batch* batch, const cz_bodies* in);
+int cz_download_bodies(cz_batch* batch, cz_bodies* out);
+
+/* One frame in the order of examples/cubedrop.go:69-75, nsteps times:
+ * Integrate + collider derived data for every body, the ordered all-pairs
+ * narrowphase (plane first, then every other body), and ResolveContacts per
+ * world.  The sequence is captured once as a CUDA graph per (nsteps, dt) and
+ * replayed.  Blocking; returns the first error status seen. */
+int cz_step(cz_batch* batch, int32_t nsteps, double dt);
+
+/* The three phases separately (blocking). */
+int cz_integrate(cz_batch* batch, double dt);                   /* rigidbody.go:213-259 */
+int cz_narrowphase(cz_batch* batch);                            /* examples/cubedrop.go:41-67 */
+int cz_resolve(cz_batch* batch, double dt);                     /* contact.go:208-222 */
+
+/* Contacts produced by the last narrowphase, in the reference's order. */
+int cz_contact_counts(cz_batch* batch, int32_t* counts /* [num_worlds] */);
+int cz_download_contacts(cz_batch* batch, int32_t world, cz_contact* out, int32_t capacity, int32_t* count);
+
+/* Per-world statistics of the last resolve: adjustPositions and
+ * adjustVelocities iterations used, and status bits. */
+int cz_world_stats(cz_batch* batch, int32_t* pos_iterations, int32_t* vel_iterations, uint32_t* status);
+
+/* ResolveContacts(maxIterations, contacts, duration) for one caller-supplied
+ * contact list (contact.go:208-222): bodies and contacts are read, resolved on
+ * the device and written back in place.  A contact with body[0] == -1 is
+ * swapped as calculateInternals does (contact.go:61-65).  Uses the batch's
+ * form; the batch must have been created with one world holding nbodies
+ * bodies and capacity >= ncontacts. */
+int cz_resolve_contacts(cz_batch* batch, int32_t max_iterations, cz_contact* contacts, int32_t ncontacts,
+                        double duration, cz_bodies* bodies);
+
+/* Tuning knobs picked by the autotuner (0 keeps the current value). */
+typedef struct cz_tuning {
+  int32_t narrowphase_threads; /* CTA size of the narrowphase */
+  int32_t resolver_contacts;   /* contacts kept in shared memory per world */
+  int32_t resolver_ctas_per_sm;/* resident resolver warps per SM */
+  int32_t integrate_threads;
+} cz_tuning;
+int cz_set_tuning(cz_batch* batch, const cz_tuning* tuning);
+int cz_get_tuning(cz_batch* batch, cz_tuning* tuning);
+
+/* Error reporting. */
+const char* cz_status_string(int status);
+const char* cz_last_error(void);
+
+/* Library information: number of kernel launches issued so far by this
+ * process (all batches), for launch accounting. */
+int64_t cz_kernel_launches(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CUBEZ_GPU_H */

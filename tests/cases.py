@@ -1,0 +1,87 @@
+"""Hand-built single-world scenes, one per narrowphase branch, with the
+contacts the reference's formulas give for them (worked out by hand from
+colliders.go, including its quirks).  Shared by the CPU oracle tests and the
+GPU parity tests."""
+import math
+
+import numpy as np
+
+from cubez_gb300 import scenes
+
+
+def quat_axis(angle, axis):
+    a = np.asarray(axis, float)
+    a = a / np.linalg.norm(a)
+    s = math.sin(angle / 2.0)
+    return np.array([math.cos(angle / 2.0), a[0] * s, a[1] * s, a[2] * s])
+
+
+def world(bodies, plane=(0.0, 1.0, 0.0, 0.0)):
+    """bodies: list of dicts with shape ('cube'|'sphere'), pos, half or r, and
+    optional quat, vel, rot, inv_mass."""
+    n = len(bodies)
+    shape = np.array([scenes.CUBE if b["shape"] == "cube" else scenes.SPHERE for b in bodies])
+    half = np.array([b.get("half", (0.0, 0.0, 0.0)) for b in bodies], float)
+    radius = np.array([b.get("r", 0.0) for b in bodies], float)
+    pos = np.array([b["pos"] for b in bodies], float)
+    quat = np.array([b.get("quat", (1.0, 0.0, 0.0, 0.0)) for b in bodies], float)
+    vel = np.array([b.get("vel", (0.0, 0.0, 0.0)) for b in bodies], float)
+    rot = np.array([b.get("rot", (0.0, 0.0, 0.0)) for b in bodies], float)
+    sc = scenes._assemble(np.array([n], np.int32), shape, half, radius, pos, quat, vel, rot, "case")
+    sc.plane = np.asarray(plane, float)
+    return sc
+
+
+FAR_PLANE = (0.0, 1.0, 0.0, -100.0)
+
+
+def cube_resting():
+    # h = 0.5 at y = 0.49: the four lower vertices are 0.01 below the plane
+    return world([dict(shape="cube", pos=(0.0, 0.49, 0.0), half=(0.5, 0.5, 0.5))])
+
+
+def sphere_resting():
+    return world([dict(shape="sphere", pos=(2.0, 0.4, -1.0), r=0.5)])
+
+
+def sphere_pair():
+    return world([dict(shape="sphere", pos=(0.0, 5.0, 0.0), r=1.0),
+                  dict(shape="sphere", pos=(1.5, 5.0, 0.0), r=1.0)], FAR_PLANE)
+
+
+def cube_sphere():
+    return world([dict(shape="cube", pos=(0.0, 5.0, 0.0), half=(1.0, 1.0, 1.0)),
+                  dict(shape="sphere", pos=(1.3, 5.0, 0.0), r=0.5)], FAR_PLANE)
+
+
+def sphere_inside_cube():
+    return world([dict(shape="cube", pos=(0.0, 5.0, 0.0), half=(1.0, 1.0, 1.0)),
+                  dict(shape="sphere", pos=(0.2, 5.0, 0.0), r=0.5, vel=(0.0, -2.0, 0.0))], FAR_PLANE)
+
+
+def cube_on_cube():
+    # B (h=0.5) rotated 45 deg about z, resting a vertex... an edge into A's top face
+    return world([dict(shape="cube", pos=(0.0, 5.0, 0.0), half=(1.0, 1.0, 1.0)),
+                  dict(shape="cube", pos=(0.1, 6.6, 0.05), half=(0.5, 0.5, 0.5),
+                       quat=quat_axis(0.3, (0.2, 0.1, 1.0)))], FAR_PLANE)
+
+
+def cube_edge_edge():
+    # two long boxes crossing edge to edge: A along x, B along z, both rolled 45 deg
+    qa = quat_axis(math.pi / 4, (1.0, 0.0, 0.0))
+    qb = quat_axis(math.pi / 4, (0.0, 0.0, 1.0))
+    d = 0.5 * math.sqrt(2.0)  # half-diagonal of a 1x1 square section
+    return world([dict(shape="cube", pos=(0.0, 5.0, 0.0), half=(2.0, 0.5, 0.5), quat=qa),
+                  dict(shape="cube", pos=(0.05, 5.0 + 2 * d - 0.04, -0.03), half=(0.5, 0.5, 2.0), quat=qb)],
+                 FAR_PLANE)
+
+
+def tilted_cube_on_plane():
+    # one vertex down: a single plane contact
+    q = quat_axis(math.atan(math.sqrt(2.0)), (1.0, 0.0, -1.0))
+    return world([dict(shape="cube", pos=(0.0, 0.85, 0.0), half=(0.5, 0.5, 0.5), quat=q)])
+
+
+ALL = {"cube_resting": cube_resting, "sphere_resting": sphere_resting, "sphere_pair": sphere_pair,
+       "cube_sphere": cube_sphere, "sphere_inside_cube": sphere_inside_cube, "cube_on_cube": cube_on_cube,
+       "cube_edge_edge": cube_edge_edge, "tilted_cube_on_plane": tilted_cube_on_plane}
