@@ -1,0 +1,398 @@
+"""Benchmark of the batched rigid-body step on GB300.
+
+Workload (default): the precision-form configuration, 16384 worlds x 32 bodies
+(16 spheres + 16 cubes; radius / half-extents U[0.25,1]; positions
+U([-6,6]x[0.5,25]x[-6,6]); velocities U[-2,2]^3; angular velocities
+U[-1,1]^3), ground plane y = 0, dt = 1/60, ResolveContacts(4 * len(contacts)).
+Synthetic seeded scenes (there is no dataset).
+
+One benchmark "step" is one 600-frame rollout of all worlds from the same
+initial state, captured as one CUDA graph (integrate -> narrowphase -> resolve
+per frame).  The metric is body-steps/s = bodies x frames / time.
+
+  value       precision form (float32 bulk, float64 islands), device time of
+              the rollout graph (CUDA events recorded on the batch stream inside
+              the graph), inputs resident in HBM
+  e2e         the same through the C ABI with host buffers: cz_upload_bodies
+              (host -> device) + cz_step + cz_download_bodies (device -> host)
+  fp64        the plain float64 form measured the same way (reported beside it)
+  roofline    the dominant kernel, algorithmic bytes per launch / its average
+              CUDA-event duration over the timed rollouts
+  cpu_baseline  the oracle (C++ restatement of the reference's float64 Go path)
+              on the host's cores, one thread per world, on a bounded sample
+
+--impl reference times the reference's CPU path (the oracle port; the Go
+reference cannot be built here) on all host cores with the same metric.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "body-steps/s: FP32+MLP warm-start vs plain FP64 on 1 GB300 at stated error"
+UNIT = "body-steps/s"
+DT = 1.0 / 60.0
+L2_BYTES = 126 * 1024 * 1024
+
+
+def _peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class Clocks:
+    """nvidia-smi sampled every 200 ms during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.out = None
+
+    def __enter__(self):
+        try:
+            self.out = open(os.path.join("/tmp", "cz_clocks_%d.csv" % os.getpid()), "w+")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.out,
+                                         stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if self.out is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        self.out.seek(0)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.out.read().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        load = [s for s in sm if s > 0.5 * max(sm)] or sm
+        return {"sm_mhz": float(np.median(load)), "sm_max_mhz": float(max(smax)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def _flush_l2():
+    import torch
+    buf = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device="cuda")
+    buf.fill_(1.0)
+    torch.cuda.synchronize()
+    del buf
+
+
+def _kinetic_energy(d, scene):
+    inv_m = scene.inverse_mass
+    v = d["velocity"]
+    w = d["rotation"]
+    iw = d["inverse_inertia_world"].reshape(-1, 3, 3).transpose(0, 2, 1)  # column-major -> row-major
+    lin = 0.5 * np.einsum("ij,ij->i", v, v) / inv_m
+    iw_inv = np.linalg.inv(iw)
+    ang = 0.5 * np.einsum("ij,ijk,ik->i", w, iw_inv, w)
+    return lin + ang
+
+
+def accuracy(scene, frames, batches):
+    """Errors of the precision form against the plain float64 form (bit-exact
+    with the oracle) on identical initial states: one-step relative error per
+    quantity, time-averaged kinetic energy and final mean height."""
+    out = {}
+    res = {}
+    for name, b in batches.items():
+        b.restore()
+        b.step(1, DT)
+        res[name] = b.download()
+    a, r = res["fp32"], res["fp64"]
+    floors = {"position": 1.0, "orientation": 1.0, "velocity": 1.0, "rotation": 1.0}
+    one = {}
+    for k, fl in floors.items():
+        den = np.maximum(np.abs(r[k]).max(axis=1), fl)
+        e = np.abs(a[k] - r[k]).max(axis=1) / den
+        one[k] = {"max": float(e.max()), "p99": float(np.quantile(e, 0.99))}
+    out["one_step_rel_error"] = one
+    ke = {name: [] for name in batches}
+    height = {}
+    seg = 30
+    for name, b in batches.items():
+        b.restore()
+        for s in range(0, frames, seg):
+            b.step(min(seg, frames - s), DT)
+            d = b.download()
+            ke[name].append(float(_kinetic_energy(d, scene).sum()))
+        height[name] = float(d["position"][:, 1].mean())
+    ke32, ke64 = np.mean(ke["fp32"]), np.mean(ke["fp64"])
+    out["ke_time_avg_rel_diff"] = float(abs(ke32 - ke64) / ke64)
+    out["mean_height_rel_diff"] = float(abs(height["fp32"] - height["fp64"]) / abs(height["fp64"]))
+    out["mean_height_fp64_m"] = height["fp64"]
+    return out
+
+
+def _alg_bytes(phase, real, nbodies, counters, frames, rollouts):
+    """Algorithmic HBM bytes per launch of a phase (the minimum each kernel must move)."""
+    launches = frames * rollouts
+    contacts = counters["contacts"] / launches
+    resolved = counters["contacts_resolved"] / launches
+    if phase == 0:  # integrate: read 13 state + 3 acc + 9+9 inertia + 3 scalars, write 13 + 3 + 9; 2 flag bytes
+        return nbodies * (62 * real + 2)
+    if phase == 1:  # narrowphase: stage 11 rows + shape, write contacts (9 reals + packed bodies)
+        return nbodies * (11 * real + 4) + contacts * (9 * real + 4)
+    # resolver: bodies in (27 reals + flag) and out (23 reals + flag), contacts in
+    return nbodies * (50 * real + 2) + resolved * (9 * real + 4)
+
+
+def run_ours(args):
+    import torch
+    ws, rank, local = _dist()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    from cubez_gb300 import _lib, scenes
+    from cubez_gb300.batch import FORM_FP32, FORM_FP64, WorldBatch
+
+    scene = scenes.precision(num_worlds=args.worlds, bodies=args.bodies, seed=3 + 1000 * rank)
+    nb = scene.num_bodies
+    frames = args.frames
+
+    def barrier():
+        if ws > 1:
+            import torch.distributed as dist
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    batches = {}
+    for name, form in (("fp32", FORM_FP32), ("fp64", FORM_FP64)):
+        b = WorldBatch.from_scene(scene, form=form, device=local)
+        b.prepare_rollout(frames, DT)  # damping factors + graph capture, outside any timed region
+        b.snapshot()
+        batches[name] = b
+
+    results = {}
+    for name in ("fp32", "fp64") if not args.fp32_only else ("fp32",):
+        b = batches[name]
+        for _ in range(args.warmup):
+            b.restore()
+            b.step_timed(frames, DT)
+        b.counters(reset=True)
+        tot_ms, ph_ms = 0.0, np.zeros(3)
+        launches0 = _lib.kernel_launches()
+        clocks = Clocks(local)
+        with clocks:
+            for _ in range(args.steps):
+                b.restore()
+                _flush_l2()
+                barrier()
+                t, ph = b.step_timed(frames, DT)
+                barrier()
+                tot_ms += t
+                ph_ms += ph
+        launches = _lib.kernel_launches() - launches0
+        cnt = b.counters()
+        ms = tot_ms / args.steps
+        if ws > 1:
+            import torch.distributed as dist
+            tt = torch.tensor([ms], device="cuda")
+            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+            ms = float(tt.item())
+        results[name] = {"ms_per_step": ms, "phase_ms": (ph_ms / args.steps).tolist(), "counters": cnt,
+                         "launches": launches, "clocks": clocks.summary(),
+                         "value": nb * frames * ws / (ms / 1e3)}
+
+    # e2e through the C ABI with host buffers (precision form)
+    e2e = None
+    if not args.no_e2e:
+        b = batches["fp32"]
+        host = {k: np.ascontiguousarray(getattr(scene, k)) for k in scene.FIELDS}
+        import ctypes as C
+        pinned = {}
+        for k, v in host.items():
+            t = torch.empty(v.nbytes, dtype=torch.uint8, pin_memory=True)
+            a = np.frombuffer(t.numpy().data, dtype=v.dtype, count=v.size).reshape(v.shape)
+            a[...] = v
+            pinned[k] = (t, a)
+        arrays = {k: a for k, (t, a) in pinned.items()}
+        for _ in range(max(1, args.warmup)):
+            b.upload(**arrays)
+            b.step(frames, DT)
+            b.download()
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            b.upload(**arrays)
+            b.step(frames, DT)
+            out = b.download()
+        barrier()
+        e2e_s = (time.perf_counter() - t0) / args.steps
+        real_h2d = 43 * 8 * nb + 2 * nb + 4 * nb + 2 * 8 * int(b.info()["padded_bodies"])
+        real_d2h = 43 * 8 * nb + 2 * nb + 4 * nb + 4
+        e2e = {"value": nb * frames * ws / e2e_s, "unit": UNIT, "h2d_bytes_per_step": real_h2d,
+               "d2h_bytes_per_step": real_d2h, "ms_per_step": e2e_s * 1e3}
+        del C, out
+
+    acc = accuracy(scene, frames, batches) if not args.no_accuracy else None
+
+    r32 = results["fp32"]
+    real = 4
+    phase_names = ["integrate", "narrowphase", "resolve"]
+    ph = r32["phase_ms"]
+    dom = int(np.argmax(ph))
+    per_launch_ms = ph[dom] / frames
+    bytes_launch = _alg_bytes(dom, real, nb, r32["counters"], frames, args.steps)
+    peak, peak_kind = _peaks()
+    achieved = bytes_launch / (per_launch_ms / 1e3) / 1e9
+    kernels = {}
+    for i, n in enumerate(phase_names):
+        bl = _alg_bytes(i, real, nb, r32["counters"], frames, args.steps)
+        pl = ph[i] / frames
+        kernels[n] = {"ms_per_launch": pl, "share": ph[i] / sum(ph), "alg_bytes_per_launch": bl,
+                      "gbs": bl / (pl / 1e3) / 1e9}
+    info = batches["fp32"].info()
+    for b in batches.values():
+        b.close()
+
+    if rank != 0:
+        return
+    cpu = None if args.no_cpu_baseline else cpu_baseline(args, scene)
+    line = {
+        "metric": METRIC, "value": r32["value"], "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": r32["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 (f64 islands)", "data": "synthetic (seeded scenes)",
+        "config": {"workload": "precision: %d worlds x %d bodies (16 spheres + 16 cubes), %d-frame rollout, "
+                               "dt=1/60, iterations 4 x contacts" % (args.worlds, args.bodies, frames),
+                   "form": "fp32 (MLP warm start not yet enabled)", "step": "one %d-frame rollout" % frames,
+                   "l2": "explicit 252 MB flush before every timed rollout; working set > L2",
+                   "parallelism": "weak: %d worlds per GPU" % args.worlds},
+        "fp64": {"value": results["fp64"]["value"] if "fp64" in results else None,
+                 "ms_per_step": results["fp64"]["ms_per_step"] if "fp64" in results else None,
+                 "phase_ms": results["fp64"]["phase_ms"] if "fp64" in results else None,
+                 "clocks": results["fp64"]["clocks"] if "fp64" in results else None},
+        "fp32_over_fp64": (r32["value"] / results["fp64"]["value"]) if "fp64" in results else None,
+        "accuracy": acc,
+        "e2e": e2e,
+        "gpu_launches": r32["launches"],
+        "clocks": r32["clocks"],
+        "roofline": {"kernel": phase_names[dom], "bound": "hbm", "achieved": achieved, "peak": peak,
+                     "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind, "traffic": None},
+        "kernels": kernels,
+        "counters_per_frame": {k: v / (frames * args.steps) for k, v in r32["counters"].items()},
+        "batch": info,
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(line))
+
+
+def cpu_baseline(args, scene):
+    """The oracle (C++ restatement of the reference's float64 path), one
+    thread per world on all host cores, on the first `cpu_worlds` worlds."""
+    from oracle.oracle import OracleBatch, hardware_threads
+    cores = os.cpu_count() or hardware_threads()
+    nw = min(args.cpu_worlds, scene.num_worlds)
+    sub = scene.subset(range(nw))
+    ob = OracleBatch(sub)
+    t0 = time.perf_counter()
+    ob.step(args.frames, DT, 4, cores)
+    el = time.perf_counter() - t0
+    return {"value": sub.num_bodies * args.frames / el, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": "%d of %d worlds x %d frames (float64 oracle, %.1f s)" % (nw, scene.num_worlds, args.frames, el)}
+
+
+def run_reference(args):
+    ws, rank, _ = _dist()
+    if rank != 0:
+        return
+    from cubez_gb300 import scenes
+    from oracle.oracle import OracleBatch, hardware_threads
+    scene = scenes.precision(num_worlds=args.worlds, bodies=args.bodies, seed=3)
+    cores = os.cpu_count() or hardware_threads()
+    nw = min(args.cpu_worlds, scene.num_worlds)
+    sub = scene.subset(range(nw))
+    for _ in range(args.warmup):
+        OracleBatch(sub).step(min(args.frames, 30), DT, 4, cores)
+    total = 0.0
+    for _ in range(args.steps):
+        ob = OracleBatch(sub)
+        t0 = time.perf_counter()
+        ob.step(args.frames, DT, 4, cores)
+        total += time.perf_counter() - t0
+    ms = total / args.steps * 1e3
+    value = sub.num_bodies * args.frames / (ms / 1e3)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded scenes)", "impl": "reference",
+        "config": {"workload": "precision: %d worlds x %d bodies, %d-frame rollout, dt=1/60; each step a sample of "
+                               "%d worlds" % (args.worlds, args.bodies, args.frames, nw),
+                   "parallelism": "host cores, one thread per world"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": "%d of %d worlds x %d frames per step (the Go reference cannot be built here; "
+                                   "its float64 path restated in C++)" % (nw, args.worlds, args.frames)},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--worlds", type=int, default=16384)
+    ap.add_argument("--bodies", type=int, default=32)
+    ap.add_argument("--frames", type=int, default=600)
+    ap.add_argument("--cpu-worlds", type=int, default=2048)
+    ap.add_argument("--fp32-only", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-accuracy", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

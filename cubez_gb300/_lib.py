@@ -64,6 +64,12 @@ SIGNATURES = {
                                       C.POINTER(Bodies)]),
     "cz_set_tuning": (C.c_int, [C.c_void_p, C.POINTER(Tuning)]),
     "cz_get_tuning": (C.c_int, [C.c_void_p, C.POINTER(Tuning)]),
+    "cz_prepare_rollout": (C.c_int, [C.c_void_p, C.c_int32, C.c_double]),
+    "cz_snapshot": (C.c_int, [C.c_void_p]),
+    "cz_restore": (C.c_int, [C.c_void_p]),
+    "cz_step_timed": (C.c_int, [C.c_void_p, C.c_int32, C.c_double, C.POINTER(C.c_double), C.c_void_p]),
+    "cz_batch_info": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "cz_counters": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32]),
     "cz_status_string": (C.c_char_p, [C.c_int]),
     "cz_last_error": (C.c_char_p, []),
     "cz_kernel_launches": (C.c_int64, []),

@@ -106,6 +106,35 @@ class WorldBatch:
     def resolve(self, dt=1.0 / 60.0):
         check(self.L.cz_resolve(self.h, float(dt)))
 
+    def prepare_rollout(self, nsteps, dt=1.0 / 60.0):
+        check(self.L.cz_prepare_rollout(self.h, int(nsteps), float(dt)))
+
+    def snapshot(self):
+        check(self.L.cz_snapshot(self.h))
+
+    def restore(self):
+        check(self.L.cz_restore(self.h))
+
+    def step_timed(self, nsteps, dt=1.0 / 60.0):
+        """Run a captured rollout; returns (total_ms, [integrate, narrowphase, resolve] ms)."""
+        tot = C.c_double(0.0)
+        ph = np.zeros(3)
+        check(self.L.cz_step_timed(self.h, int(nsteps), float(dt), C.byref(tot), _ptr(ph)))
+        return tot.value, ph
+
+    def counters(self, reset=False):
+        a = np.zeros(4, np.int64)
+        check(self.L.cz_counters(self.h, _ptr(a), 1 if reset else 0))
+        return {"contacts": int(a[0]), "pos_iterations": int(a[1]), "vel_iterations": int(a[2]),
+                "contacts_resolved": int(a[3])}
+
+    def info(self):
+        a = np.zeros(9, np.int64)
+        check(self.L.cz_batch_info(self.h, _ptr(a)))
+        keys = ("bodies", "padded_bodies", "contact_slots", "real_bytes", "sms", "narrowphase_ctas", "resolver_ctas",
+                "narrowphase_smem", "resolver_smem")
+        return dict(zip(keys, (int(x) for x in a)))
+
     # ---------------------------------------------------------------- results
     def contact_counts(self):
         c = np.zeros(self.num_worlds, np.int32)

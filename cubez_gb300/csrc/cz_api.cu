@@ -72,6 +72,7 @@ struct cz_batch {
   int* d_order = nullptr;
   unsigned* d_queue = nullptr;
   uint32_t* d_status = nullptr;
+  unsigned long long* d_counters = nullptr;
   int* d_h2p = nullptr;
   double* d_stage = nullptr;
   uint8_t* d_stage_u8 = nullptr;
@@ -100,6 +101,16 @@ struct cz_batch {
 
   // graph cache: (nsteps, dt) -> executable graph
   std::map<std::pair<int, double>, cudaGraphExec_t> graphs;
+  // rollouts with event-record nodes between the phases (cz_step_timed)
+  struct Timed {
+    cudaGraphExec_t exec = nullptr;
+    std::vector<cudaEvent_t> ev;  // 3 * nsteps + 1
+  };
+  std::map<std::pair<int, double>, Timed> timed;
+  // on-device copy of the body state (cz_snapshot / cz_restore)
+  void* snap_body = nullptr;
+  uint8_t* snap_u8 = nullptr;  // awake, can_sleep
+  double snap_pow_dt = std::nan("");
 
   cz::HostView view() const {
     cz::HostView v;
@@ -126,6 +137,7 @@ struct cz_batch {
     v.order = d_order;
     v.queue = d_queue;
     v.status = d_status;
+    v.counters = d_counters;
     for (int i = 0; i < 4; ++i) v.plane[i] = plane[i];
     v.iter_mult = iter_mult;
     v.max_iterations = max_iterations;
@@ -140,9 +152,13 @@ void free_batch(cz_batch* b) {
   if (!b) return;
   cudaSetDevice(b->device);
   for (auto& kv : b->graphs) cudaGraphExecDestroy(kv.second);
-  void* dev[] = {b->body, b->awake, b->can_sleep, b->shape, b->d_bstart, b->d_bcount, b->d_ccap, b->d_ccount,
+  for (auto& kv : b->timed) {
+    cudaGraphExecDestroy(kv.second.exec);
+    for (cudaEvent_t e : kv.second.ev) cudaEventDestroy(e);
+  }
+  void* dev[] = {b->snap_body, b->snap_u8, b->body, b->awake, b->can_sleep, b->shape, b->d_bstart, b->d_bcount, b->d_ccap, b->d_ccount,
                  b->d_cstart, b->d_wstatus, b->d_piters, b->d_viters, b->contact, b->cbodies, b->work, b->wbodies,
-                 b->d_order, b->d_queue, b->d_status, b->d_h2p, b->d_stage, b->d_stage_u8, b->d_stage_i32,
+                 b->d_order, b->d_queue, b->d_status, b->d_counters, b->d_h2p, b->d_stage, b->d_stage_u8, b->d_stage_i32,
                  b->d_cstage, b->d_cstage_b, b->d_pow};
   for (void* p : dev)
     if (p) cudaFree(p);
@@ -241,6 +257,11 @@ int configure(cz_batch* b) {
   b->rs_grid = std::max(b->rs_grid, 1);
   for (auto& kv : b->graphs) cudaGraphExecDestroy(kv.second);
   b->graphs.clear();
+  for (auto& kv : b->timed) {
+    cudaGraphExecDestroy(kv.second.exec);
+    for (cudaEvent_t e : kv.second.ev) cudaEventDestroy(e);
+  }
+  b->timed.clear();
   return CZ_OK;
 }
 
@@ -346,7 +367,8 @@ int cz_batch_create(const cz_batch_desc* d, cz_batch** out) {
        dmalloc((void**)&b->d_order, sizeof(int) * W);
   ok = ok && dmalloc(&b->contact, R * cz::C_NROWS * C) && dmalloc((void**)&b->cbodies, sizeof(int) * C);
   ok = ok && dmalloc(&b->work, R * cz::W_NROWS * C) && dmalloc((void**)&b->wbodies, sizeof(int) * C);
-  ok = ok && dmalloc((void**)&b->d_queue, 4 * sizeof(unsigned)) && dmalloc((void**)&b->d_status, sizeof(uint32_t));
+  ok = ok && dmalloc((void**)&b->d_queue, 4 * sizeof(unsigned)) && dmalloc((void**)&b->d_status, sizeof(uint32_t)) &&
+       dmalloc((void**)&b->d_counters, 4 * sizeof(unsigned long long));
   ok = ok && dmalloc((void**)&b->d_h2p, sizeof(int) * std::max<long long>(nb, 1));
   ok = ok && dmalloc((void**)&b->d_stage, sizeof(double) * cz::SG_NDOUBLES * std::max<long long>(nb, 1)) &&
        dmalloc((void**)&b->d_stage_u8, 2 * std::max<long long>(nb, 1)) &&
@@ -354,6 +376,7 @@ int cz_batch_create(const cz_batch_desc* d, cz_batch** out) {
   ok = ok && dmalloc((void**)&b->d_cstage, sizeof(double) * cz::C_NROWS * b->max_cap) &&
        dmalloc((void**)&b->d_cstage_b, sizeof(int) * b->max_cap);
   ok = ok && dmalloc((void**)&b->d_pow, sizeof(double) * 2 * P);
+  ok = ok && dmalloc(&b->snap_body, R * cz::B_NROWS * P) && dmalloc((void**)&b->snap_u8, 2 * P);
   if (!ok) return bail(fail(CZ_ERR_CUDA, "device allocation failed"));
   ok = cudaMallocHost((void**)&b->h_stage, sizeof(double) * cz::SG_NDOUBLES * std::max<long long>(nb, 1)) ==
            cudaSuccess &&
@@ -375,6 +398,7 @@ int cz_batch_create(const cz_batch_desc* d, cz_batch** out) {
       cudaMemsetAsync(b->d_viters, 0, sizeof(int) * W, s) != cudaSuccess ||
       cudaMemsetAsync(b->d_queue, 0, 4 * sizeof(unsigned), s) != cudaSuccess ||
       cudaMemsetAsync(b->d_status, 0, sizeof(uint32_t), s) != cudaSuccess ||
+      cudaMemsetAsync(b->d_counters, 0, 4 * sizeof(unsigned long long), s) != cudaSuccess ||
       cudaMemsetAsync(b->cbodies, 0xFF, sizeof(int) * C, s) != cudaSuccess ||
       cudaMemcpyAsync(b->d_bstart, b->bstart.data(), sizeof(int) * W, cudaMemcpyHostToDevice, s) != cudaSuccess ||
       cudaMemcpyAsync(b->d_bcount, bcount.data(), sizeof(int) * W, cudaMemcpyHostToDevice, s) != cudaSuccess ||
@@ -535,6 +559,79 @@ int cz_resolve(cz_batch* b, double dt) {
   return finish(b);
 }
 
+// Capture (once per (nsteps, dt)) the plain rollout graph.
+static int get_graph(cz_batch* b, int nsteps, double dt, cudaGraphExec_t* out) {
+  auto key = std::make_pair(nsteps, dt);
+  auto it = b->graphs.find(key);
+  if (it != b->graphs.end()) {
+    *out = it->second;
+    return CZ_OK;
+  }
+  CZ_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+  const long long before = g_launches.load();
+  int cst = CZ_OK;
+  for (int s = 0; s < nsteps && cst == CZ_OK; ++s) {
+    cst = launch_integrate(b, dt);
+    if (!cst) cst = launch_narrowphase(b);
+    if (!cst) cst = launch_resolve(b, dt);
+  }
+  g_launches.store(before);  // captured launches are counted when the graph runs
+  cudaGraph_t graph = nullptr;
+  cudaError_t e = cudaStreamEndCapture(b->stream, &graph);
+  if (cst != CZ_OK) {
+    if (graph) cudaGraphDestroy(graph);
+    return cst;
+  }
+  if (e != cudaSuccess) return fail(CZ_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+  cudaGraphExec_t exec = nullptr;
+  e = cudaGraphInstantiate(&exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (e != cudaSuccess) return fail(CZ_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+  b->graphs.emplace(key, exec);
+  *out = exec;
+  return CZ_OK;
+}
+
+// Capture the rollout with event-record nodes around every phase.
+static int get_timed(cz_batch* b, int nsteps, double dt, cz_batch::Timed** out) {
+  auto key = std::make_pair(nsteps, dt);
+  auto it = b->timed.find(key);
+  if (it != b->timed.end()) {
+    *out = &it->second;
+    return CZ_OK;
+  }
+  cz_batch::Timed t;
+  t.ev.resize(3 * (size_t)nsteps + 1);
+  for (auto& e : t.ev) CZ_CUDA(cudaEventCreate(&e));
+  CZ_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+  const long long before = g_launches.load();
+  int cst = cudaEventRecordWithFlags(t.ev[0], b->stream, cudaEventRecordExternal) == cudaSuccess ? CZ_OK : CZ_ERR_CUDA;
+  for (int s = 0; s < nsteps && cst == CZ_OK; ++s) {
+    cst = launch_integrate(b, dt);
+    if (!cst && cudaEventRecordWithFlags(t.ev[3 * s + 1], b->stream, cudaEventRecordExternal) != cudaSuccess) cst = CZ_ERR_CUDA;
+    if (!cst) cst = launch_narrowphase(b);
+    if (!cst && cudaEventRecordWithFlags(t.ev[3 * s + 2], b->stream, cudaEventRecordExternal) != cudaSuccess) cst = CZ_ERR_CUDA;
+    if (!cst) cst = launch_resolve(b, dt);
+    if (!cst && cudaEventRecordWithFlags(t.ev[3 * s + 3], b->stream, cudaEventRecordExternal) != cudaSuccess) cst = CZ_ERR_CUDA;
+  }
+  g_launches.store(before);
+  cudaGraph_t graph = nullptr;
+  cudaError_t e = cudaStreamEndCapture(b->stream, &graph);
+  if (cst != CZ_OK || e != cudaSuccess) {
+    if (graph) cudaGraphDestroy(graph);
+    for (auto& ev : t.ev) cudaEventDestroy(ev);
+    return fail(CZ_ERR_CUDA, "timed graph capture failed");
+  }
+  e = cudaGraphInstantiate(&t.exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (e != cudaSuccess) {
+    for (auto& ev : t.ev) cudaEventDestroy(ev);
+    return fail(CZ_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+  }
+  *out = &b->timed.emplace(key, std::move(t)).first->second;
+  return CZ_OK;
+}
+
 int cz_step(cz_batch* b, int32_t nsteps, double dt) {
   if (!b || nsteps < 0) return fail(CZ_ERR_BAD_ARG, "cz_step: bad argument");
   if (nsteps == 0) return CZ_OK;
@@ -542,35 +639,22 @@ int cz_step(cz_batch* b, int32_t nsteps, double dt) {
   int st = ensure_pows(b, dt);
   if (st) return st;
   if ((st = reset_status(b))) return st;
-  auto key = std::make_pair((int)nsteps, dt);
-  auto it = b->graphs.find(key);
-  if (it == b->graphs.end()) {
-    // capture the rollout once: per step, integrate -> narrowphase -> resolve
-    CZ_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
-    const long long before = g_launches.load();
-    int cst = CZ_OK;
-    for (int s = 0; s < nsteps && cst == CZ_OK; ++s) {
-      cst = launch_integrate(b, dt);
-      if (!cst) cst = launch_narrowphase(b);
-      if (!cst) cst = launch_resolve(b, dt);
-    }
-    g_launches.store(before);  // captured launches are counted when the graph runs
-    cudaGraph_t graph = nullptr;
-    cudaError_t e = cudaStreamEndCapture(b->stream, &graph);
-    if (cst != CZ_OK) {
-      if (graph) cudaGraphDestroy(graph);
-      return cst;
-    }
-    if (e != cudaSuccess) return fail(CZ_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
-    cudaGraphExec_t exec = nullptr;
-    e = cudaGraphInstantiate(&exec, graph, 0);
-    cudaGraphDestroy(graph);
-    if (e != cudaSuccess) return fail(CZ_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
-    it = b->graphs.emplace(key, exec).first;
-  }
-  CZ_CUDA(cudaGraphLaunch(it->second, b->stream));
+  cudaGraphExec_t exec = nullptr;
+  if ((st = get_graph(b, nsteps, dt, &exec))) return st;
+  CZ_CUDA(cudaGraphLaunch(exec, b->stream));
   g_launches += 3LL * nsteps;
   return finish(b);
+}
+
+int cz_prepare_rollout(cz_batch* b, int32_t nsteps, double dt) {
+  if (!b || nsteps <= 0) return fail(CZ_ERR_BAD_ARG, "cz_prepare_rollout: bad argument");
+  CZ_CUDA(cudaSetDevice(b->device));
+  int st = ensure_pows(b, dt);
+  if (st) return st;
+  cudaGraphExec_t exec = nullptr;
+  if ((st = get_graph(b, nsteps, dt, &exec))) return st;
+  cz_batch::Timed* t = nullptr;
+  return get_timed(b, nsteps, dt, &t);
 }
 
 int cz_contact_counts(cz_batch* b, int32_t* counts) {
@@ -683,6 +767,82 @@ int cz_resolve_contacts(cz_batch* b, int32_t max_iterations, cz_contact* contact
     contacts[k].penetration = c[cz::C_PEN];
   }
   return st;
+}
+
+int cz_snapshot(cz_batch* b) {
+  if (!b) return fail(CZ_ERR_BAD_ARG, "cz_snapshot: null batch");
+  CZ_CUDA(cudaSetDevice(b->device));
+  const size_t bytes = b->ops->real_size * cz::B_NROWS * b->nb_pad;
+  CZ_CUDA(cudaMemcpyAsync(b->snap_body, b->body, bytes, cudaMemcpyDeviceToDevice, b->stream));
+  CZ_CUDA(cudaMemcpyAsync(b->snap_u8, b->awake, b->nb_pad, cudaMemcpyDeviceToDevice, b->stream));
+  CZ_CUDA(cudaMemcpyAsync(b->snap_u8 + b->nb_pad, b->can_sleep, b->nb_pad, cudaMemcpyDeviceToDevice, b->stream));
+  CZ_CUDA(cudaStreamSynchronize(b->stream));
+  b->snap_pow_dt = b->pow_dt;
+  return CZ_OK;
+}
+
+int cz_restore(cz_batch* b) {
+  if (!b) return fail(CZ_ERR_BAD_ARG, "cz_restore: null batch");
+  CZ_CUDA(cudaSetDevice(b->device));
+  const size_t bytes = b->ops->real_size * cz::B_NROWS * b->nb_pad;
+  CZ_CUDA(cudaMemcpyAsync(b->body, b->snap_body, bytes, cudaMemcpyDeviceToDevice, b->stream));
+  CZ_CUDA(cudaMemcpyAsync(b->awake, b->snap_u8, b->nb_pad, cudaMemcpyDeviceToDevice, b->stream));
+  CZ_CUDA(cudaMemcpyAsync(b->can_sleep, b->snap_u8 + b->nb_pad, b->nb_pad, cudaMemcpyDeviceToDevice, b->stream));
+  CZ_CUDA(cudaStreamSynchronize(b->stream));
+  b->pow_dt = b->snap_pow_dt;  // the snapshot holds the damping factors of its own dt
+  return CZ_OK;
+}
+
+int cz_step_timed(cz_batch* b, int32_t nsteps, double dt, double* total_ms, double* phase_ms) {
+  if (!b || nsteps <= 0) return fail(CZ_ERR_BAD_ARG, "cz_step_timed: bad argument");
+  CZ_CUDA(cudaSetDevice(b->device));
+  int st = ensure_pows(b, dt);
+  if (st) return st;
+  if ((st = reset_status(b))) return st;
+  cz_batch::Timed* t = nullptr;
+  if ((st = get_timed(b, nsteps, dt, &t))) return st;
+  CZ_CUDA(cudaGraphLaunch(t->exec, b->stream));
+  g_launches += 3LL * nsteps;
+  st = finish(b);
+  double ph[3] = {0, 0, 0};
+  for (int s = 0; s < nsteps; ++s)
+    for (int k = 0; k < 3; ++k) {
+      float ms = 0.f;
+      CZ_CUDA(cudaEventElapsedTime(&ms, t->ev[3 * s + k], t->ev[3 * s + k + 1]));
+      ph[k] += ms;
+    }
+  float tot = 0.f;
+  CZ_CUDA(cudaEventElapsedTime(&tot, t->ev[0], t->ev[3 * (size_t)nsteps]));
+  if (total_ms) *total_ms = tot;
+  if (phase_ms)
+    for (int k = 0; k < 3; ++k) phase_ms[k] = ph[k];
+  return st;
+}
+
+int cz_counters(cz_batch* b, int64_t* out, int32_t reset) {
+  if (!b) return fail(CZ_ERR_BAD_ARG, "cz_counters: null batch");
+  CZ_CUDA(cudaSetDevice(b->device));
+  unsigned long long c[4] = {0, 0, 0, 0};
+  CZ_CUDA(cudaMemcpyAsync(c, b->d_counters, sizeof c, cudaMemcpyDeviceToHost, b->stream));
+  if (reset) CZ_CUDA(cudaMemsetAsync(b->d_counters, 0, sizeof c, b->stream));
+  CZ_CUDA(cudaStreamSynchronize(b->stream));
+  if (out)
+    for (int i = 0; i < 4; ++i) out[i] = (int64_t)c[i];
+  return CZ_OK;
+}
+
+int cz_batch_info(cz_batch* b, int64_t* info) {
+  if (!b || !info) return fail(CZ_ERR_BAD_ARG, "cz_batch_info: null argument");
+  info[0] = b->nb;
+  info[1] = b->nb_pad;
+  info[2] = b->nc_total;
+  info[3] = (int64_t)b->ops->real_size;
+  info[4] = b->sm_count;
+  info[5] = b->np_grid;
+  info[6] = b->rs_grid;
+  info[7] = (int64_t)b->np_smem;
+  info[8] = (int64_t)b->rs_smem;
+  return CZ_OK;
 }
 
 }  // extern "C"

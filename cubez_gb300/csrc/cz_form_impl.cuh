@@ -35,6 +35,7 @@ static BatchView<R> view_of(const HostView& h) {
   v.order = h.order;
   v.queue = h.queue;
   v.status = h.status;
+  v.counters = h.counters;
   v.plane_nx = (R)h.plane[0];
   v.plane_ny = (R)h.plane[1];
   v.plane_nz = (R)h.plane[2];

@@ -33,6 +33,7 @@ struct HostView {
   const int* order;
   unsigned* queue;
   uint32_t* status;
+  unsigned long long* counters;
   double plane[4];
   int iter_mult;
   int max_iterations;

@@ -627,6 +627,7 @@ __global__ void __launch_bounds__(256) k_narrowphase(BatchView<R> v, int nbs) {
     }
     if (tid == 0) {
       v.contact_count[w] = out;
+      atomicAdd(&v.counters[0], (unsigned long long)out);
       if (out > cap) {
         atomicOr(&v.world_status[w], ST_CAPACITY);
         atomicOr(v.status, ST_CAPACITY);
@@ -1143,6 +1144,9 @@ __global__ void __launch_bounds__(32) k_resolve(BatchView<R> v, int nbs, int cs,
     if (lane == 0) {
       v.pos_iters[w] = pos_used;
       v.vel_iters[w] = used;
+      atomicAdd(&v.counters[1], (unsigned long long)pos_used);
+      atomicAdd(&v.counters[2], (unsigned long long)used);
+      atomicAdd(&v.counters[3], (unsigned long long)C);
     }
     if (v.contact_writeback) {
       // the caller's Contact values after ResolveContacts (penetration,

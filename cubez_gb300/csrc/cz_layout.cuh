@@ -90,6 +90,8 @@ template <class R> struct BatchView {
   const int* order;     // world queue: worlds in decreasing cost
   unsigned* queue;      // [0] narrowphase, [1] resolver, [2..3] spare
   uint32_t* status;     // batch status word
+  unsigned long long* counters;  // [0] contacts generated, [1] adjustPositions iterations,
+                                 // [2] adjustVelocities iterations, [3] contacts resolved
   R plane_nx, plane_ny, plane_nz, plane_offset;
   int iter_mult;        // ResolveContacts(len(contacts) * iter_mult)
   int max_iterations;   // >= 0 overrides len(contacts) * iter_mult

@@ -103,8 +103,8 @@ typedef struct cz_contact {
   double penetration;
 } cz_contact;
 
-/* Create / destroy a batch of worlds on one GPU.  Allocates all device memory
- * up front; no later call allocates. */
+/* Create / destroy a batch of worlds on one GPU.  All device buffers of the
+ * batch are allocated here. */
 int cz_batch_create(const cz_batch_desc* desc, cz_batch** out);
 int cz_batch_destroy(cz_batch* batch);
 
@@ -120,6 +120,10 @@ int cz_download_bodies(cz_batch* batch, cz_bodies* out);
  * world.  The sequence is captured once as a CUDA graph per (nsteps, dt) and
  * replayed.  Blocking; returns the first error status seen. */
 int cz_step(cz_batch* batch, int32_t nsteps, double dt);
+
+/* Compute the damping factors for dt and capture the rollout graphs of
+ * cz_step / cz_step_timed for nsteps without running them. */
+int cz_prepare_rollout(cz_batch* batch, int32_t nsteps, double dt);
 
 /* The three phases separately (blocking). */
 int cz_integrate(cz_batch* batch, double dt);                   /* rigidbody.go:213-259 */
@@ -142,6 +146,26 @@ int cz_world_stats(cz_batch* batch, int32_t* pos_iterations, int32_t* vel_iterat
  * bodies and capacity >= ncontacts. */
 int cz_resolve_contacts(cz_batch* batch, int32_t max_iterations, cz_contact* contacts, int32_t ncontacts,
                         double duration, cz_bodies* bodies);
+
+/* Save the whole device body state / put it back (device-to-device copies;
+ * the rollout benchmark restarts every timed rollout from the same state). */
+int cz_snapshot(cz_batch* batch);
+int cz_restore(cz_batch* batch);
+
+/* cz_step with CUDA events recorded on the batch stream around every phase
+ * inside the captured rollout: total_ms = whole rollout, phase_ms[0..2] =
+ * integrate, narrowphase, resolve summed over the steps. */
+int cz_step_timed(cz_batch* batch, int32_t nsteps, double dt, double* total_ms, double* phase_ms);
+
+/* Running totals since creation or the last reset: [0] contacts generated,
+ * [1] adjustPositions iterations, [2] adjustVelocities iterations, [3]
+ * contacts resolved.  reset != 0 zeroes them after reading. */
+int cz_counters(cz_batch* batch, int64_t* out /* [4] */, int32_t reset);
+
+/* Sizes: [0] bodies, [1] padded bodies, [2] contact slots, [3] bytes per real,
+ * [4] SMs, [5] narrowphase CTAs, [6] resolver CTAs, [7] narrowphase shared
+ * bytes, [8] resolver shared bytes. */
+int cz_batch_info(cz_batch* batch, int64_t* info /* [9] */);
 
 /* Tuning knobs picked by the autotuner (0 keeps the current value). */
 typedef struct cz_tuning {

@@ -38,6 +38,9 @@ def lib():
         L.orc_contact_count.argtypes = [C.c_void_p, C.c_int]
         L.orc_get_contacts.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
         L.orc_get_stats.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+        L.orc_set_contacts.argtypes = [C.c_void_p, C.c_int] + [C.c_void_p] * 6 + [C.c_int]
+        L.orc_resolve_fixed.argtypes = [C.c_void_p, C.c_double, C.c_int]
+        L.orc_get_resolved.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
         L.orc_real_equal.argtypes = [C.c_double, C.c_double]
         L.orc_quat_len.restype = C.c_double
         L.orc_quat_len.argtypes = [C.c_void_p]
@@ -122,6 +125,27 @@ class OracleBatch:
         pen = np.zeros(n)
         self.L.orc_get_contacts(self.h, world, _ptr(b), _ptr(p), _ptr(nn), _ptr(pen), n)
         return {"bodies": b, "point": p, "normal": nn, "penetration": pen}
+
+    def set_contacts(self, world, c):
+        """Replace world's contact list (dict of bodies, point, normal,
+        penetration, friction, restitution arrays)."""
+        n = len(c["penetration"])
+        self._c = {k: np.ascontiguousarray(c[k], dtype=np.int32 if k == "bodies" else np.float64)
+                   for k in ("bodies", "point", "normal", "penetration", "friction", "restitution")}
+        k = self._c
+        self.L.orc_set_contacts(self.h, world, _ptr(k["bodies"]), _ptr(k["point"]), _ptr(k["normal"]),
+                                _ptr(k["penetration"]), _ptr(k["friction"]), _ptr(k["restitution"]), n)
+
+    def resolve_fixed(self, max_iterations, dt=1.0 / 60.0):
+        return self.L.orc_resolve_fixed(self.h, dt, max_iterations)
+
+    def resolved_contacts(self, world):
+        n = self.L.orc_contact_count(self.h, world)
+        b = np.zeros((n, 2), np.int32)
+        nn = np.zeros((n, 3))
+        pen = np.zeros(n)
+        self.L.orc_get_resolved(self.h, world, _ptr(b), _ptr(nn), _ptr(pen), n)
+        return {"bodies": b, "normal": nn, "penetration": pen}
 
     def stats(self):
         W = self.scene.num_worlds

@@ -46,6 +46,10 @@ struct BatchBase {
   virtual int contactCount(int w) = 0;
   virtual int contacts(int w, int32_t* b2, double* p3, double* n3, double* pen, int cap) = 0;
   virtual void stats(int32_t* c, int32_t* pit, int32_t* vit) = 0;
+  virtual void setContacts(int w, const int32_t* b2, const double* p3, const double* n3, const double* pen,
+                           const double* fric, const double* rest, int n) = 0;
+  virtual uint32_t resolveFixed(double dt, int maxIter) = 0;
+  virtual int resolved(int w, int32_t* b2, double* n3, double* pen, int cap) = 0;
 };
 
 template <class R, class W> struct Batch : BatchBase {
@@ -198,6 +202,51 @@ template <class R, class W> struct Batch : BatchBase {
     }
   }
 
+  void setContacts(int w, const int32_t* b2, const double* p3, const double* n3, const double* pen,
+                   const double* fric, const double* rest, int n) override {
+    work[w].clear();
+    for (int i = 0; i < n; ++i) {
+      Contact<R> c = NewContact<R>();
+      c.body[0] = b2[2 * i];
+      c.body[1] = b2[2 * i + 1];
+      for (int k = 0; k < 3; ++k) {
+        c.point[k] = (R)p3[3 * i + k];
+        c.normal[k] = (R)n3[3 * i + k];
+      }
+      c.penetration = (R)pen[i];
+      c.friction = (R)fric[i];
+      c.restitution = (R)rest[i];
+      work[w].push_back(c);
+    }
+    generated[w] = work[w];
+  }
+
+  // ResolveContacts(maxIter, contacts, dt) on the contact lists set above
+  uint32_t resolveFixed(double dt, int maxIter) override {
+    uint32_t err = 0;
+    for (int w = 0; w < nworlds; ++w) {
+      Resolver<R, W> rs;
+      rs.bodies = &bodies[start[w]];
+      rs.ResolveContacts(maxIter, work[w], (R)dt, count[w]);
+      st[w].posIterations = rs.posIterations;
+      st[w].velIterations = rs.velIterations;
+      err |= rs.err;
+    }
+    return err;
+  }
+
+  int resolved(int w, int32_t* b2, double* n3, double* pen, int cap) override {
+    const auto& cs = work[w];
+    int n = (int)cs.size();
+    for (int i = 0; i < n && i < cap; ++i) {
+      b2[2 * i] = cs[i].body[0];
+      b2[2 * i + 1] = cs[i].body[1];
+      for (int k = 0; k < 3; ++k) n3[3 * i + k] = (double)cs[i].normal[k];
+      pen[i] = (double)cs[i].penetration;
+    }
+    return n;
+  }
+
   int contactCount(int w) override { return (int)generated[w].size(); }
 
   int contacts(int w, int32_t* b2, double* p3, double* n3, double* pen, int cap) override {
@@ -246,6 +295,16 @@ int orc_get_contacts(void* h, int w, int32_t* b2, double* p3, double* n3, double
   return static_cast<BatchBase*>(h)->contacts(w, b2, p3, n3, pen, cap);
 }
 void orc_get_stats(void* h, int32_t* c, int32_t* pit, int32_t* vit) { static_cast<BatchBase*>(h)->stats(c, pit, vit); }
+void orc_set_contacts(void* h, int w, const int32_t* b2, const double* p3, const double* n3, const double* pen,
+                      const double* fric, const double* rest, int n) {
+  static_cast<BatchBase*>(h)->setContacts(w, b2, p3, n3, pen, fric, rest, n);
+}
+int orc_resolve_fixed(void* h, double dt, int maxIter) {
+  return (int)static_cast<BatchBase*>(h)->resolveFixed(dt, maxIter);
+}
+int orc_get_resolved(void* h, int w, int32_t* b2, double* n3, double* pen, int cap) {
+  return static_cast<BatchBase*>(h)->resolved(w, b2, n3, pen, cap);
+}
 int orc_hardware_threads() { return (int)std::thread::hardware_concurrency(); }
 
 // ---- math layer entry points for the known-answer tests (math/*_test.go)

@@ -1,0 +1,78 @@
+"""The seeded scene generator: deterministic, distributions as configured,
+body setup as the reference's helpers compute it."""
+import numpy as np
+
+from cubez_gb300 import scenes
+
+
+def test_deterministic_and_order_independent():
+    a = scenes.mixed(num_worlds=64, seed=9)
+    b = scenes.mixed(num_worlds=64, seed=9)
+    for k in a.FIELDS:
+        np.testing.assert_array_equal(getattr(a, k), getattr(b, k))
+    # world w does not depend on how many worlds are generated
+    c = scenes.mixed(num_worlds=16, seed=9)
+    np.testing.assert_array_equal(a.counts[:16], c.counts)
+    n16 = int(c.counts.sum())
+    np.testing.assert_array_equal(a.position[:n16], c.position)
+    d = scenes.mixed(num_worlds=64, seed=10)
+    assert not np.array_equal(a.position[:10], d.position[:10])
+
+
+def test_mixed_distributions():
+    s = scenes.mixed(num_worlds=4096)
+    assert s.counts.min() >= 8 and s.counts.max() <= 64
+    assert abs(s.counts.mean() - 36) < 1.0
+    frac = (s.shape == scenes.SPHERE).mean()
+    assert 0.48 < frac < 0.52
+    sph = s.shape == scenes.SPHERE
+    assert s.radius[sph].min() >= 0.25 and s.radius[sph].max() <= 1.0
+    assert s.half_size[~sph].min() >= 0.25 and s.half_size[~sph].max() <= 1.0
+    assert s.position[:, 1].min() >= 0.5 and s.position[:, 1].max() <= 25.0
+    assert np.abs(s.velocity).max() <= 2.0 and np.abs(s.rotation).max() <= 1.0
+    np.testing.assert_allclose(np.linalg.norm(s.orientation, axis=1), 1.0, atol=1e-12)
+
+
+def test_precision_split_and_setup():
+    s = scenes.precision(num_worlds=128)
+    assert np.all(s.counts == 32)
+    per_world = (s.shape == scenes.SPHERE).reshape(128, 32).sum(axis=1)
+    assert np.all(per_world == 16)
+    cube = s.shape == scenes.CUBE
+    h = s.half_size[cube]
+    mass = 8.0 * h[:, 0] * h[:, 1] * h[:, 2]
+    np.testing.assert_allclose(1.0 / s.inverse_mass[cube], mass, rtol=1e-15)
+    # inverse of SetBlockInertiaTensor: 1 / (0.3 m (hy^2 + hz^2)) on the diagonal
+    np.testing.assert_allclose(s.inverse_inertia[cube][:, 0], 1.0 / (0.3 * mass * (h[:, 1] ** 2 + h[:, 2] ** 2)),
+                               rtol=1e-14)
+    sph = ~cube
+    r = s.radius[sph]
+    m = 4.0 / 3.0 * np.pi * r ** 3
+    np.testing.assert_allclose(s.inverse_inertia[sph][:, 4], 1.0 / (0.4 * m * r * r), rtol=1e-14)
+    assert np.all(s.can_sleep == 0) and np.all(s.is_awake == 1)
+    np.testing.assert_array_equal(s.acceleration[:, 1], -9.8)
+    np.testing.assert_array_equal(s.linear_damping, 0.95)
+    np.testing.assert_array_equal(s.angular_damping, 0.8)
+
+
+def test_cubedrop_and_piles():
+    c = scenes.cubedrop()
+    assert c.num_worlds == 1 and c.num_bodies == 20 and np.all(c.shape == scenes.CUBE)
+    assert c.half_size.min() >= 0.5 and c.position[:, 1].min() >= 1.0
+    np.testing.assert_array_equal(c.velocity, 0.0)
+    p = scenes.piles(num_worlds=2)
+    assert np.all(p.counts == 1024)
+    assert p.half_size.min() >= 0.3 and p.half_size.max() <= 0.6
+    q = p.orientation
+    tilt = 2 * np.arccos(np.clip(np.abs(q[:, 0]), 0, 1))
+    assert tilt.max() <= 0.2 + 1e-9
+    bottom = p.position[:, 1] - 0.6
+    assert bottom.min() >= 0.5 - 0.1 - 1e-12
+
+
+def test_subset():
+    s = scenes.mixed(num_worlds=10, seed=4)
+    sub = s.subset([2, 5])
+    assert sub.num_worlds == 2
+    np.testing.assert_array_equal(sub.position, np.concatenate([s.position[s.world_slice(2)],
+                                                                s.position[s.world_slice(5)]]))
