@@ -202,9 +202,18 @@ def run_ours(args):
             dist.barrier()
         torch.cuda.synchronize()
 
+    from cubez_gb300 import autotune
     batches = {}
+    tuning = {}
     for name, form in (("fp32", FORM_FP32), ("fp64", FORM_FP64)):
         b = WorldBatch.from_scene(scene, form=form, device=local)
+        if args.autotune:
+            # tune on a settled state (half-way through the rollout), untimed
+            b.step(frames // 2, DT)
+            b.snapshot()
+            cfg, _ = autotune.tune(b, frames=args.tune_frames, dt=DT)
+            tuning[name] = cfg
+            b.upload(scene)
         b.prepare_rollout(frames, DT)  # damping factors + graph capture, outside any timed region
         b.snapshot()
         batches[name] = b
@@ -318,6 +327,7 @@ def run_ours(args):
         "kernels": kernels,
         "counters_per_frame": {k: v / (frames * args.steps) for k, v in r32["counters"].items()},
         "batch": info,
+        "tuning": tuning,
         "cpu_baseline": cpu,
     }
     print(json.dumps(line))
@@ -384,6 +394,8 @@ def main():
     ap.add_argument("--frames", type=int, default=600)
     ap.add_argument("--cpu-worlds", type=int, default=2048)
     ap.add_argument("--fp32-only", action="store_true")
+    ap.add_argument("--autotune", type=int, default=1)
+    ap.add_argument("--tune-frames", type=int, default=30)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-accuracy", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")

@@ -1,0 +1,62 @@
+"""Autotuner for the batched step's launch shapes.
+
+Searches, on the caller's own batch and scene state, over
+  * resolver lanes per world G (worlds per warp = 32 / G),
+  * the resolver's shared-memory contact tile (contacts per world kept on chip),
+  * the narrowphase CTA size,
+timing a short captured rollout for each candidate with CUDA events, and
+leaves the batch set to the fastest.  Every candidate computes the same bits
+(the parity tests run all lanes settings), so tuning changes only speed.
+
+The state is restored from the batch snapshot before every trial, so the
+search is reproducible; the snapshot should hold a representative
+(settled) state.
+"""
+import itertools
+
+DEFAULT_LANES = (4, 8, 16, 32)
+DEFAULT_TILES = (64, 96, 128, 192)
+DEFAULT_NP_THREADS = (64, 128, 256)
+
+
+def tune(batch, frames=30, dt=1.0 / 60.0, lanes=DEFAULT_LANES, tiles=DEFAULT_TILES, np_threads=DEFAULT_NP_THREADS,
+         repeats=1, log=None):
+    """Returns (best_config, trials); the batch is left at best_config."""
+    trials = []
+
+    def measure():
+        best = None
+        for _ in range(repeats):
+            batch.restore()
+            total, phases = batch.step_timed(frames, dt)
+            best = phases if best is None or phases.sum() < best.sum() else best
+        return best
+
+    # narrowphase CTA size first (independent of the resolver settings)
+    np_best, np_time = None, None
+    for t in np_threads:
+        batch.set_tuning(narrowphase_threads=t)
+        ph = measure()
+        trials.append({"narrowphase_threads": t, "narrowphase_ms": float(ph[1])})
+        if np_time is None or ph[1] < np_time:
+            np_best, np_time = t, ph[1]
+    batch.set_tuning(narrowphase_threads=np_best)
+    best, best_ms = None, None
+    for g, cs in itertools.product(lanes, tiles):
+        try:
+            batch.set_tuning(resolver_lanes=g, resolver_contacts=cs)
+        except Exception as e:  # a tile that does not fit in shared memory
+            trials.append({"resolver_lanes": g, "resolver_contacts": cs, "error": str(e)})
+            continue
+        ph = measure()
+        cfg = batch.get_tuning()
+        trials.append({"resolver_lanes": g, "resolver_contacts": cfg["resolver_contacts"],
+                       "resolver_ms": float(ph[2])})
+        if log:
+            log("lanes=%d tile=%d resolve %.3f ms" % (g, cfg["resolver_contacts"], ph[2]))
+        if best_ms is None or ph[2] < best_ms:
+            best, best_ms = (g, cfg["resolver_contacts"]), ph[2]
+    batch.set_tuning(resolver_lanes=best[0], resolver_contacts=best[1])
+    batch.restore()
+    cfg = batch.get_tuning()
+    return cfg, trials

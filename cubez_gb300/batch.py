@@ -163,12 +163,14 @@ class WorldBatch:
         return {"pos_iterations": pi, "vel_iterations": vi, "status": st}
 
     # ---------------------------------------------------------------- tuning
-    def set_tuning(self, narrowphase_threads=0, resolver_contacts=0, resolver_ctas_per_sm=0, integrate_threads=0):
-        t = _lib.Tuning(narrowphase_threads, resolver_contacts, resolver_ctas_per_sm, integrate_threads)
+    def set_tuning(self, narrowphase_threads=0, resolver_contacts=0, resolver_ctas_per_sm=0, integrate_threads=0,
+                   resolver_lanes=0):
+        t = _lib.Tuning(narrowphase_threads, resolver_contacts, resolver_ctas_per_sm, integrate_threads, resolver_lanes)
         check(self.L.cz_set_tuning(self.h, C.byref(t)))
 
     def get_tuning(self):
         t = _lib.Tuning()
         check(self.L.cz_get_tuning(self.h, C.byref(t)))
         return {"narrowphase_threads": t.narrowphase_threads, "resolver_contacts": t.resolver_contacts,
-                "resolver_ctas_per_sm": t.resolver_ctas_per_sm, "integrate_threads": t.integrate_threads}
+                "resolver_ctas_per_sm": t.resolver_ctas_per_sm, "integrate_threads": t.integrate_threads,
+                "resolver_lanes": t.resolver_lanes}

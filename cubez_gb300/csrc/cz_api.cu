@@ -70,6 +70,7 @@ struct cz_batch {
   void* work = nullptr;
   int* wbodies = nullptr;
   int* d_order = nullptr;
+  int* d_order_rs = nullptr;
   unsigned* d_queue = nullptr;
   uint32_t* d_status = nullptr;
   unsigned long long* d_counters = nullptr;
@@ -97,6 +98,7 @@ struct cz_batch {
 
   // tuning
   int np_threads = 128, np_grid = 1, rs_cs = 128, rs_grid = 1, rs_ctas_per_sm = 0, int_threads = 256;
+  int rs_lanes = 8;  // lanes per world in the resolver (32 / rs_lanes worlds per warp)
   size_t np_smem = 0, rs_smem = 0;
 
   // graph cache: (nsteps, dt) -> executable graph
@@ -135,6 +137,7 @@ struct cz_batch {
     v.work_bodies = wbodies;
     v.nc_total = nc_total;
     v.order = d_order;
+    v.order_rs = d_order_rs;
     v.queue = d_queue;
     v.status = d_status;
     v.counters = d_counters;
@@ -142,11 +145,61 @@ struct cz_batch {
     v.iter_mult = iter_mult;
     v.max_iterations = max_iterations;
     v.contact_writeback = 0;
+    v.uniform_material = 1;
     return v;
   }
 };
 
 namespace {
+
+// Resolver queue for the next frame: worlds in decreasing adjustPositions +
+// adjustVelocities iterations of this frame (a counting sort in one CTA), so
+// that the worlds sharing a warp in lockstep have similar work.  The order of
+// independent worlds does not change any result.
+constexpr int kReorderBuckets = 2048;
+__global__ void __launch_bounds__(1024) k_reorder(const int* __restrict__ pos_it, const int* __restrict__ vel_it,
+                                                  int W, int* __restrict__ order) {
+  __shared__ int hist[kReorderBuckets];
+  __shared__ int wsum[32];
+  const int tid = threadIdx.x;
+  for (int i = tid; i < kReorderBuckets; i += blockDim.x) hist[i] = 0;
+  __syncthreads();
+  for (int w = tid; w < W; w += blockDim.x) {
+    const int key = min(pos_it[w] + vel_it[w], kReorderBuckets - 1);
+    atomicAdd(&hist[kReorderBuckets - 1 - key], 1);
+  }
+  __syncthreads();
+  // exclusive scan of 2048 buckets, two per thread
+  const int a = hist[2 * tid], c = hist[2 * tid + 1];
+  int x = a + c;
+  const int lane = tid & 31, wid = tid >> 5;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, x, d);
+    if (lane >= d) x += y;
+  }
+  if (lane == 31) wsum[wid] = x;
+  __syncthreads();
+  if (wid == 0) {
+    int t = wsum[lane];
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, t, d);
+      if (lane >= d) t += y;
+    }
+    wsum[lane] = t;
+  }
+  __syncthreads();
+  const int excl = x - (a + c) + (wid > 0 ? wsum[wid - 1] : 0);
+  __syncthreads();
+  hist[2 * tid] = excl;
+  hist[2 * tid + 1] = excl + a;
+  __syncthreads();
+  for (int w = tid; w < W; w += blockDim.x) {
+    const int key = min(pos_it[w] + vel_it[w], kReorderBuckets - 1);
+    order[atomicAdd(&hist[kReorderBuckets - 1 - key], 1)] = w;
+  }
+}
 
 void free_batch(cz_batch* b) {
   if (!b) return;
@@ -158,7 +211,7 @@ void free_batch(cz_batch* b) {
   }
   void* dev[] = {b->snap_body, b->snap_u8, b->body, b->awake, b->can_sleep, b->shape, b->d_bstart, b->d_bcount, b->d_ccap, b->d_ccount,
                  b->d_cstart, b->d_wstatus, b->d_piters, b->d_viters, b->contact, b->cbodies, b->work, b->wbodies,
-                 b->d_order, b->d_queue, b->d_status, b->d_counters, b->d_h2p, b->d_stage, b->d_stage_u8, b->d_stage_i32,
+                 b->d_order, b->d_order_rs, b->d_queue, b->d_status, b->d_counters, b->d_h2p, b->d_stage, b->d_stage_u8, b->d_stage_i32,
                  b->d_cstage, b->d_cstage_b, b->d_pow};
   for (void* p : dev)
     if (p) cudaFree(p);
@@ -216,6 +269,8 @@ int ensure_pows(cz_batch* b, double dt) {
   return CZ_OK;
 }
 
+int launches_per_step(const cz_batch* b) { return 3 + (b->num_worlds > 32 / b->rs_lanes ? 1 : 0); }
+
 int launch_integrate(cz_batch* b, double dt) {
   CZ_CUDA(b->ops->integrate(b->view(), dt, std::pow(0.5, dt), b->int_threads, b->stream));
   g_launches++;
@@ -229,9 +284,14 @@ int launch_narrowphase(cz_batch* b) {
 }
 int launch_resolve(cz_batch* b, double dt, const cz::HostView* override_view = nullptr) {
   CZ_CUDA(cudaMemsetAsync(b->d_queue + 1, 0, sizeof(unsigned), b->stream));
-  CZ_CUDA(b->ops->resolve(override_view ? *override_view : b->view(), b->nbs, b->rs_cs, b->rs_grid, b->rs_smem, dt,
-                          b->stream));
+  CZ_CUDA(b->ops->resolve(override_view ? *override_view : b->view(), b->nbs, b->rs_cs, b->rs_lanes, b->rs_grid,
+                          b->rs_smem, dt, b->stream));
   g_launches++;
+  if (b->num_worlds > 32 / b->rs_lanes) {
+    k_reorder<<<1, 1024, 0, b->stream>>>(b->d_piters, b->d_viters, b->num_worlds, b->d_order_rs);
+    CZ_CUDA(cudaGetLastError());
+    g_launches++;
+  }
   return CZ_OK;
 }
 
@@ -239,20 +299,21 @@ int configure(cz_batch* b) {
   // resolver shared-memory tile: shrink the contact capacity until it fits
   int cs = std::min<long long>(b->rs_cs, round_up(b->max_cap, 32));
   cs = std::max(cs, 32);
-  while (cs > 32 && b->ops->rs_smem(b->nbs, cs) > b->smem_optin) cs -= 32;
+  while (cs > 32 && b->ops->rs_smem(b->nbs, cs, b->rs_lanes) > b->smem_optin) cs -= 32;
   b->rs_cs = cs;
-  b->rs_smem = b->ops->rs_smem(b->nbs, cs);
+  b->rs_smem = b->ops->rs_smem(b->nbs, cs, b->rs_lanes);
   b->np_smem = b->ops->np_smem(b->nbs);
   if (b->np_smem > b->smem_optin || b->rs_smem > b->smem_optin)
     return fail(CZ_ERR_BODY_LIMIT, "world too large for the shared-memory tiles");
-  CZ_CUDA(b->ops->prepare(b->np_smem, b->rs_smem));
+  CZ_CUDA(b->ops->prepare(b->np_smem, b->rs_smem, b->rs_lanes));
   int npb = 0, rsb = 0;
-  CZ_CUDA(b->ops->occupancy(&npb, b->np_threads, b->np_smem, &rsb, b->rs_smem));
+  CZ_CUDA(b->ops->occupancy(&npb, b->np_threads, b->np_smem, &rsb, b->rs_smem, b->rs_lanes));
   npb = std::max(npb, 1);
   rsb = std::max(rsb, 1);
   if (b->rs_ctas_per_sm > 0) rsb = std::min(rsb, b->rs_ctas_per_sm);
   b->np_grid = (int)std::min<long long>(b->num_worlds, (long long)npb * b->sm_count);
-  b->rs_grid = (int)std::min<long long>(b->num_worlds, (long long)rsb * b->sm_count);
+  const long long groups = (b->num_worlds + 32 / b->rs_lanes - 1) / (32 / b->rs_lanes);
+  b->rs_grid = (int)std::min<long long>(groups, (long long)rsb * b->sm_count);
   b->np_grid = std::max(b->np_grid, 1);
   b->rs_grid = std::max(b->rs_grid, 1);
   for (auto& kv : b->graphs) cudaGraphExecDestroy(kv.second);
@@ -344,7 +405,8 @@ int cz_batch_create(const cz_batch_desc* d, cz_batch** out) {
   b->nc_total = std::max<long long>(nc, 4);
   b->nbs = (int)std::max<long long>(round_up(b->max_n, 4), 4);
   b->np_threads = b->max_n >= 256 ? 256 : 128;
-  b->rs_cs = d->form == CZ_FORM_FP64 ? 128 : 192;
+  b->rs_cs = d->form == CZ_FORM_FP64 ? 96 : 128;
+  b->rs_lanes = d->form == CZ_FORM_FP64 ? 4 : 8;
   // world queue: decreasing body count (pair work grows as n^2)
   std::vector<int> order(b->num_worlds);
   std::iota(order.begin(), order.end(), 0);
@@ -364,7 +426,7 @@ int cz_batch_create(const cz_batch_desc* d, cz_batch** out) {
        dmalloc((void**)&b->d_ccap, sizeof(int) * W) && dmalloc((void**)&b->d_ccount, sizeof(int) * W) &&
        dmalloc((void**)&b->d_cstart, sizeof(long long) * W) && dmalloc((void**)&b->d_wstatus, sizeof(uint32_t) * W) &&
        dmalloc((void**)&b->d_piters, sizeof(int) * W) && dmalloc((void**)&b->d_viters, sizeof(int) * W) &&
-       dmalloc((void**)&b->d_order, sizeof(int) * W);
+       dmalloc((void**)&b->d_order, sizeof(int) * W) && dmalloc((void**)&b->d_order_rs, sizeof(int) * W);
   ok = ok && dmalloc(&b->contact, R * cz::C_NROWS * C) && dmalloc((void**)&b->cbodies, sizeof(int) * C);
   ok = ok && dmalloc(&b->work, R * cz::W_NROWS * C) && dmalloc((void**)&b->wbodies, sizeof(int) * C);
   ok = ok && dmalloc((void**)&b->d_queue, 4 * sizeof(unsigned)) && dmalloc((void**)&b->d_status, sizeof(uint32_t)) &&
@@ -406,6 +468,7 @@ int cz_batch_create(const cz_batch_desc* d, cz_batch** out) {
       cudaMemcpyAsync(b->d_cstart, b->cstart.data(), sizeof(long long) * W, cudaMemcpyHostToDevice, s) !=
           cudaSuccess ||
       cudaMemcpyAsync(b->d_order, order.data(), sizeof(int) * W, cudaMemcpyHostToDevice, s) != cudaSuccess ||
+      cudaMemcpyAsync(b->d_order_rs, order.data(), sizeof(int) * W, cudaMemcpyHostToDevice, s) != cudaSuccess ||
       (nb > 0 &&
        cudaMemcpyAsync(b->d_h2p, b->h2p.data(), sizeof(int) * nb, cudaMemcpyHostToDevice, s) != cudaSuccess) ||
       cudaStreamSynchronize(s) != cudaSuccess)
@@ -433,6 +496,11 @@ int cz_set_tuning(cz_batch* b, const cz_tuning* t) {
     b->np_threads = t->narrowphase_threads;
   }
   if (t->resolver_contacts > 0) b->rs_cs = (int)round_up(t->resolver_contacts, 32);
+  if (t->resolver_lanes > 0) {
+    if (t->resolver_lanes != 4 && t->resolver_lanes != 8 && t->resolver_lanes != 16 && t->resolver_lanes != 32)
+      return fail(CZ_ERR_BAD_ARG, "resolver_lanes must be 4, 8, 16 or 32");
+    b->rs_lanes = t->resolver_lanes;
+  }
   if (t->resolver_ctas_per_sm > 0) b->rs_ctas_per_sm = t->resolver_ctas_per_sm;
   if (t->integrate_threads > 0) {
     if (t->integrate_threads % 32 != 0 || t->integrate_threads > 256)
@@ -448,6 +516,7 @@ int cz_get_tuning(cz_batch* b, cz_tuning* t) {
   t->resolver_contacts = b->rs_cs;
   t->resolver_ctas_per_sm = b->rs_grid / std::max(b->sm_count, 1);
   t->integrate_threads = b->int_threads;
+  t->resolver_lanes = b->rs_lanes;
   return CZ_OK;
 }
 
@@ -642,7 +711,7 @@ int cz_step(cz_batch* b, int32_t nsteps, double dt) {
   cudaGraphExec_t exec = nullptr;
   if ((st = get_graph(b, nsteps, dt, &exec))) return st;
   CZ_CUDA(cudaGraphLaunch(exec, b->stream));
-  g_launches += 3LL * nsteps;
+  g_launches += (long long)launches_per_step(b) * nsteps;
   return finish(b);
 }
 
@@ -745,6 +814,7 @@ int cz_resolve_contacts(cz_batch* b, int32_t max_iterations, cz_contact* contact
   cz::HostView v = b->view();
   v.max_iterations = std::max(max_iterations, 0);
   v.contact_writeback = 1;
+  v.uniform_material = 0;
   if ((st = launch_resolve(b, duration, &v))) return st;
   st = finish(b);
   if (st != CZ_OK && st != CZ_ERR_FRICTIONLESS) return st;
@@ -802,7 +872,7 @@ int cz_step_timed(cz_batch* b, int32_t nsteps, double dt, double* total_ms, doub
   cz_batch::Timed* t = nullptr;
   if ((st = get_timed(b, nsteps, dt, &t))) return st;
   CZ_CUDA(cudaGraphLaunch(t->exec, b->stream));
-  g_launches += 3LL * nsteps;
+  g_launches += (long long)launches_per_step(b) * nsteps;
   st = finish(b);
   double ph[3] = {0, 0, 0};
   for (int s = 0; s < nsteps; ++s)

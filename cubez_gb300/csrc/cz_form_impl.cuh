@@ -33,6 +33,7 @@ static BatchView<R> view_of(const HostView& h) {
   v.work_bodies = h.work_bodies;
   v.nc_total = h.nc_total;
   v.order = h.order;
+  v.order_rs = h.order_rs;
   v.queue = h.queue;
   v.status = h.status;
   v.counters = h.counters;
@@ -43,6 +44,7 @@ static BatchView<R> view_of(const HostView& h) {
   v.iter_mult = h.iter_mult;
   v.max_iterations = h.max_iterations;
   v.contact_writeback = h.contact_writeback;
+  v.uniform_material = h.uniform_material;
   return v;
 }
 
@@ -153,12 +155,25 @@ __global__ void k_set_rows(BatchView<R> v, int row, int nrows, const double* __r
 }
 
 static size_t np_smem(int nbs) { return np_smem_bytes<R>(nbs); }
-static size_t rs_smem(int nbs, int cs) { return rs_smem_bytes<R, W>(nbs, cs); }
+static size_t rs_smem(int nbs, int cs, int lanes) { return (size_t)(32 / lanes) * rs_slot_bytes<R, W>(nbs, cs); }
 
-static cudaError_t prepare(size_t np, size_t rs) {
+// the resolver instantiation for G lanes per world
+static const void* resolve_fn(int lanes) {
+  switch (lanes) {
+    case 4: return (const void*)k_resolve<R, W, 4>;
+    case 8: return (const void*)k_resolve<R, W, 8>;
+    case 16: return (const void*)k_resolve<R, W, 16>;
+    case 32: return (const void*)k_resolve<R, W, 32>;
+    default: return nullptr;
+  }
+}
+
+static cudaError_t prepare(size_t np, size_t rs, int lanes) {
   cudaError_t e = cudaFuncSetAttribute(k_narrowphase<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)np);
   if (e != cudaSuccess) return e;
-  return cudaFuncSetAttribute(k_resolve<R, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rs);
+  const void* f = resolve_fn(lanes);
+  if (!f) return cudaErrorInvalidValue;
+  return cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rs);
 }
 
 static cudaError_t integrate(const HostView& h, double dt, double bias, int threads, cudaStream_t s) {
@@ -173,8 +188,16 @@ static cudaError_t narrowphase(const HostView& h, int nbs, int threads, int grid
   return cudaGetLastError();
 }
 
-static cudaError_t resolve(const HostView& h, int nbs, int cs, int grid, size_t smem, double dt, cudaStream_t s) {
-  k_resolve<R, W><<<grid, 32, smem, s>>>(view_of(h), nbs, cs, (R)dt);
+static cudaError_t resolve(const HostView& h, int nbs, int cs, int lanes, int grid, size_t smem, double dt,
+                           cudaStream_t s) {
+  const BatchView<R> v = view_of(h);
+  switch (lanes) {
+    case 4: k_resolve<R, W, 4><<<grid, 32, smem, s>>>(v, nbs, cs, (R)dt); break;
+    case 8: k_resolve<R, W, 8><<<grid, 32, smem, s>>>(v, nbs, cs, (R)dt); break;
+    case 16: k_resolve<R, W, 16><<<grid, 32, smem, s>>>(v, nbs, cs, (R)dt); break;
+    case 32: k_resolve<R, W, 32><<<grid, 32, smem, s>>>(v, nbs, cs, (R)dt); break;
+    default: return cudaErrorInvalidValue;
+  }
   return cudaGetLastError();
 }
 
@@ -192,10 +215,12 @@ static cudaError_t download(const HostView& h, double* sg, uint8_t* u8, int* i32
   return cudaGetLastError();
 }
 
-static cudaError_t occupancy(int* npb, int np_threads, size_t nps, int* rsb, size_t rss) {
+static cudaError_t occupancy(int* npb, int np_threads, size_t nps, int* rsb, size_t rss, int lanes) {
   cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(npb, k_narrowphase<R>, np_threads, nps);
   if (e != cudaSuccess) return e;
-  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(rsb, k_resolve<R, W>, 32, rss);
+  const void* f = resolve_fn(lanes);
+  if (!f) return cudaErrorInvalidValue;
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(rsb, f, 32, rss);
 }
 
 static cudaError_t contacts_out(const HostView& h, long long start, int count, double* sg, int* bodies,

@@ -31,6 +31,7 @@ struct HostView {
   int* work_bodies;
   long long nc_total;
   const int* order;
+  const int* order_rs;
   unsigned* queue;
   uint32_t* status;
   unsigned long long* counters;
@@ -38,6 +39,7 @@ struct HostView {
   int iter_mult;
   int max_iterations;
   int contact_writeback;
+  int uniform_material;
 };
 
 // Staging layout of host body data on the device (doubles, field blocks of n):
@@ -49,16 +51,18 @@ enum StageBlock : int {
 struct FormOps {
   size_t real_size;
   size_t (*np_smem)(int nbs);
-  size_t (*rs_smem)(int nbs, int cs);
-  cudaError_t (*prepare)(size_t np_smem, size_t rs_smem);  // function attributes
+  size_t (*rs_smem)(int nbs, int cs, int lanes);  // per CTA (one warp, 32 / lanes worlds)
+  cudaError_t (*prepare)(size_t np_smem, size_t rs_smem, int lanes);  // function attributes
   cudaError_t (*integrate)(const HostView& v, double dt, double sleep_bias, int threads, cudaStream_t s);
   cudaError_t (*narrowphase)(const HostView& v, int nbs, int threads, int grid, size_t smem, cudaStream_t s);
-  cudaError_t (*resolve)(const HostView& v, int nbs, int cs, int grid, size_t smem, double dt, cudaStream_t s);
+  cudaError_t (*resolve)(const HostView& v, int nbs, int cs, int lanes, int grid, size_t smem, double dt,
+                         cudaStream_t s);
   cudaError_t (*upload)(const HostView& v, const double* stage, const uint8_t* u8, const int* i32, const int* h2p,
                         int nb, int has_iw, int has_lfa, cudaStream_t s);
   cudaError_t (*download)(const HostView& v, double* stage, uint8_t* u8, int* i32, const int* h2p, int nb,
                           cudaStream_t s);
-  cudaError_t (*occupancy)(int* np_blocks, int np_threads, size_t np_smem, int* rs_blocks, size_t rs_smem);
+  cudaError_t (*occupancy)(int* np_blocks, int np_threads, size_t np_smem, int* rs_blocks, size_t rs_smem,
+                           int lanes);
   // contacts: device rows <-> AoS doubles staging (10 doubles + 2 ints per contact)
   cudaError_t (*contacts_out)(const HostView& v, long long start, int count, double* stage, int* bodies,
                               cudaStream_t s);

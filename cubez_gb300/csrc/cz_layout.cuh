@@ -30,16 +30,16 @@ enum BodyRow : int {
 // Narrowphase output (Contact fields set by the colliders).
 enum ContactRow : int { C_PX, C_PY, C_PZ, C_NX, C_NY, C_NZ, C_PEN, C_FRIC, C_REST, C_NROWS };
 
-// Resolver working set (Contact's private fields, contact.go:38-50).
+// Resolver working set (Contact's private fields, contact.go:38-50).  The
+// third basis column is not stored: calculateContactBasis (contact.go:118-156)
+// derives it from the normal and the second column by the same formulas.
 enum WorkRow : int {
   W_PEN, W_DDV,
   W_NX, W_NY, W_NZ,
   W_TYX, W_TYY, W_TYZ,
-  W_TZX, W_TZY, W_TZZ,
   W_R0X, W_R0Y, W_R0Z,
   W_R1X, W_R1Y, W_R1Z,
   W_CVX, W_CVY, W_CVZ,
-  W_FRIC, W_REST,
   W_NROWS
 };
 
@@ -87,7 +87,8 @@ template <class R> struct BatchView {
   R* work;              // [W_NROWS][nc_total]
   int* work_bodies;     // [nc_total]
   long long nc_total;
-  const int* order;     // world queue: worlds in decreasing cost
+  const int* order;     // narrowphase queue: worlds in decreasing body count
+  const int* order_rs;  // resolver queue: worlds in decreasing iterations of the previous frame
   unsigned* queue;      // [0] narrowphase, [1] resolver, [2..3] spare
   uint32_t* status;     // batch status word
   unsigned long long* counters;  // [0] contacts generated, [1] adjustPositions iterations,
@@ -96,6 +97,7 @@ template <class R> struct BatchView {
   int iter_mult;        // ResolveContacts(len(contacts) * iter_mult)
   int max_iterations;   // >= 0 overrides len(contacts) * iter_mult
   int contact_writeback; // copy the resolved contacts back to the contact rows
+  int uniform_material;  // every contact has the colliders' friction 0.9 / restitution 0.1
 };
 
 }  // namespace cz

@@ -173,6 +173,7 @@ typedef struct cz_tuning {
   int32_t resolver_contacts;   /* contacts kept in shared memory per world */
   int32_t resolver_ctas_per_sm;/* resident resolver warps per SM */
   int32_t integrate_threads;
+  int32_t resolver_lanes;      /* lanes per world in the resolver: 4, 8, 16 or 32 */
 } cz_tuning;
 int cz_set_tuning(cz_batch* batch, const cz_tuning* tuning);
 int cz_get_tuning(cz_batch* batch, cz_tuning* tuning);

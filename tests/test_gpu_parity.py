@@ -127,3 +127,28 @@ def test_precision_scene_fp64_step(cuda_lib):
     ref.step(120, DT, threads=8)
     assert_bodies_equal(gpu.download(), ref.bodies())
     assert_contacts_equal(gpu, ref, scene.num_worlds)
+
+
+@pytest.mark.parametrize("form", [0, 1])
+@pytest.mark.parametrize("lanes", [4, 8, 16, 32])
+def test_resolver_lanes_per_world_bit_exact(form, lanes, cuda_lib):
+    """Every lanes-per-world setting of the resolver gives the oracle's bits;
+    a small shared-memory contact tile forces some worlds onto the global
+    working rows as well."""
+    scene = scenes.mixed(num_worlds=40, seed=26)
+    ref = OracleBatch(scene, form=ORC_FP64 if form == 0 else ORC_FP32)
+    ref.step(150, DT)  # settle: piles with many contacts
+    st = ref.bodies()
+    moved = scene.copy()
+    for k in ("position", "orientation", "velocity", "rotation"):
+        setattr(moved, k, st[k])
+    gpu, ref = _pair(moved, form, cuda_lib)
+    gpu.set_tuning(resolver_lanes=lanes, resolver_contacts=32)
+    assert gpu.get_tuning()["resolver_lanes"] == lanes
+    gpu.step(30, DT)
+    ref.step(30, DT)
+    assert_bodies_equal(gpu.download(), ref.bodies())
+    gs, rs = gpu.stats(), ref.stats()
+    assert np.array_equal(gs["pos_iterations"], rs["pos_iterations"])
+    assert np.array_equal(gs["vel_iterations"], rs["vel_iterations"])
+    assert rs["contacts"].max() > 32  # some worlds exceed the shared-memory tile
