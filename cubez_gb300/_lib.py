@@ -62,6 +62,8 @@ SIGNATURES = {
     "cz_world_stats": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "cz_resolve_contacts": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_int32, C.c_double,
                                       C.POINTER(Bodies)]),
+    "cz_resolve_contacts_static": (C.c_int, [C.c_int32, C.c_int32, C.c_void_p, C.c_int32, C.c_double,
+                                             C.POINTER(Bodies), C.c_int32, C.c_void_p]),
     "cz_set_tuning": (C.c_int, [C.c_void_p, C.POINTER(Tuning)]),
     "cz_get_tuning": (C.c_int, [C.c_void_p, C.POINTER(Tuning)]),
     "cz_prepare_rollout": (C.c_int, [C.c_void_p, C.c_int32, C.c_double]),

@@ -42,6 +42,11 @@ long long round_up(long long x, long long m) { return (x + m - 1) / m * m; }
 
 }  // namespace
 
+int cz::set_error(int status, const char* what, cudaError_t e) {
+  g_last_error = std::string(what) + (e != cudaSuccess ? std::string(": ") + cudaGetErrorString(e) : "");
+  return status;
+}
+
 struct cz_batch {
   const cz::FormOps* ops = nullptr;
   int form = 0;

@@ -257,6 +257,7 @@ const FormOps CZ_FORM_OBJ = {sizeof(CZ_R),
                              CZ_FORM_NS::occupancy,
                              CZ_FORM_NS::contacts_out,
                              CZ_FORM_NS::contacts_in,
-                             CZ_FORM_NS::set_rows};
+                             CZ_FORM_NS::set_rows,
+                             CZ_FORM_NS::resolve_fn};
 
 }  // namespace cz

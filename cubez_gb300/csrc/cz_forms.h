@@ -69,9 +69,13 @@ struct FormOps {
   cudaError_t (*contacts_in)(const HostView& v, long long start, int count, const double* stage, const int* bodies,
                              cudaStream_t s);
   cudaError_t (*set_rows)(const HostView& v, int row, int nrows, const double* src, cudaStream_t s);
+  const void* (*resolve_kernel)(int lanes);  // the resolver instantiation for `lanes` lanes per world
 };
 
 extern const FormOps kFormFP64;
 extern const FormOps kFormFP32;
+
+// Records the message cz_last_error() returns; returns status.
+int set_error(int status, const char* what, cudaError_t e);
 
 }  // namespace cz

@@ -167,6 +167,27 @@ int cz_counters(cz_batch* batch, int64_t* out /* [4] */, int32_t reset);
  * bytes, [8] resolver shared bytes. */
 int cz_batch_info(cz_batch* batch, int64_t* info /* [9] */);
 
+/* ResolveContacts for one world without allocating any memory.  This entry
+ * point has no counterpart in the reference; it serves callers that cannot
+ * call cudaMalloc (a frame loop that must not allocate once it runs, or a host
+ * that only hands the library pointers into device memory it already owns).
+ * Same semantics as cz_resolve_contacts, but every array is in DEVICE memory
+ * owned by the caller: `contacts` is a device array of cz_contact, and
+ * `bodies` is a host struct whose pointers point to device arrays (position,
+ * orientation, velocity, rotation, inverse_inertia, inverse_mass, is_awake
+ * are required; inverse_inertia_world, last_frame_acceleration and motion are
+ * optional as in cz_upload_bodies).  Results are written back into those
+ * arrays, and the call synchronises `stream` (a cudaStream_t; NULL = the
+ * legacy default stream) before it returns.
+ *   Scratch: a statically reserved device array of about 1.8 MB that every
+ *   GPU loading the library holds until exit; hence the limits of at most 64
+ *   bodies and 8192 contacts (CZ_ERR_BAD_ARG beyond).  The first call on a
+ *   device looks up the array's device address (set-up); make that first call
+ *   before any stream capture.  All calls share the array, so calls whose GPU
+ *   work overlaps race on it: serialise them. */
+int cz_resolve_contacts_static(int32_t form, int32_t max_iterations, cz_contact* contacts, int32_t ncontacts,
+                               double duration, const cz_bodies* bodies, int32_t nbodies, void* stream);
+
 /* Tuning knobs picked by the autotuner (0 keeps the current value). */
 typedef struct cz_tuning {
   int32_t narrowphase_threads; /* CTA size of the narrowphase */
