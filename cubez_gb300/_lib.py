@@ -64,6 +64,17 @@ SIGNATURES = {
                                       C.POINTER(Bodies)]),
     "cz_resolve_contacts_static": (C.c_int, [C.c_int32, C.c_int32, C.c_void_p, C.c_int32, C.c_double,
                                              C.POINTER(Bodies), C.c_int32, C.c_void_p]),
+    "cz_set_warm_start": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "cz_harvest": (C.c_int, [C.c_void_p, C.c_int32, C.c_double, C.c_int32, C.c_void_p, C.c_void_p, C.c_int64,
+                             C.POINTER(C.c_int64)]),
+    "cz_mlp_create": (C.c_int, [C.c_int32, C.c_uint64, C.POINTER(C.c_void_p)]),
+    "cz_mlp_destroy": (C.c_int, [C.c_void_p]),
+    "cz_mlp_get_params": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "cz_mlp_set_params": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "cz_mlp_set_data": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_int32]),
+    "cz_mlp_train": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_float, C.c_uint64, C.c_void_p]),
+    "cz_mlp_loss_and_grad": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(C.c_float), C.c_void_p]),
+    "cz_mlp_predict": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]),
     "cz_set_tuning": (C.c_int, [C.c_void_p, C.POINTER(Tuning)]),
     "cz_get_tuning": (C.c_int, [C.c_void_p, C.POINTER(Tuning)]),
     "cz_prepare_rollout": (C.c_int, [C.c_void_p, C.c_int32, C.c_double]),

@@ -123,10 +123,10 @@ class WorldBatch:
         return tot.value, ph
 
     def counters(self, reset=False):
-        a = np.zeros(4, np.int64)
+        a = np.zeros(6, np.int64)
         check(self.L.cz_counters(self.h, _ptr(a), 1 if reset else 0))
         return {"contacts": int(a[0]), "pos_iterations": int(a[1]), "vel_iterations": int(a[2]),
-                "contacts_resolved": int(a[3])}
+                "contacts_resolved": int(a[3]), "warm_fallbacks": int(a[4]), "warm_worlds": int(a[5])}
 
     def info(self):
         a = np.zeros(9, np.int64)

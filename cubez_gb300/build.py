@@ -14,8 +14,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libcubez_gb300.so")
-UNITS = ["cz_fp64.cu", "cz_fp32.cu", "cz_api.cu", "cz_static.cu"]
-HEADERS = ["cz_math.cuh", "cz_layout.cuh", "cz_kernels.cuh", "cz_resolve.cuh", "cz_form_impl.cuh", "cz_forms.h"]
+UNITS = ["cz_fp64.cu", "cz_fp32.cu", "cz_api.cu", "cz_static.cu", "cz_mlp.cu"]
+HEADERS = ["cz_math.cuh", "cz_layout.cuh", "cz_kernels.cuh", "cz_resolve.cuh", "cz_form_impl.cuh", "cz_forms.h",
+           "cz_mlp.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "--fmad=false", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-fno-fast-math"]
 

@@ -104,6 +104,13 @@ struct cz_batch {
   // tuning
   int np_threads = 128, np_grid = 1, rs_cs = 128, rs_grid = 1, rs_ctas_per_sm = 0, int_threads = 256;
   int rs_lanes = 8;  // lanes per world in the resolver (32 / rs_lanes worlds per warp)
+  int mode = 0;      // resolver mode: 0 plain, 1 harvest, 2 learned warm start
+  cz::MlpDev mlp{};  // device copy of the warm-start network
+  void* mlp_mem = nullptr;
+  float* hv_features = nullptr;
+  float* hv_labels = nullptr;
+  unsigned long long* hv_count = nullptr;
+  long long hv_cap = 0;
   size_t np_smem = 0, rs_smem = 0;
 
   // graph cache: (nsteps, dt) -> executable graph
@@ -151,6 +158,12 @@ struct cz_batch {
     v.max_iterations = max_iterations;
     v.contact_writeback = 0;
     v.uniform_material = 1;
+    v.mode = mode;
+    v.mlp = mlp;
+    v.hv_features = hv_features;
+    v.hv_labels = hv_labels;
+    v.hv_count = hv_count;
+    v.hv_cap = hv_cap;
     return v;
   }
 };
@@ -214,7 +227,7 @@ void free_batch(cz_batch* b) {
     cudaGraphExecDestroy(kv.second.exec);
     for (cudaEvent_t e : kv.second.ev) cudaEventDestroy(e);
   }
-  void* dev[] = {b->snap_body, b->snap_u8, b->body, b->awake, b->can_sleep, b->shape, b->d_bstart, b->d_bcount, b->d_ccap, b->d_ccount,
+  void* dev[] = {b->mlp_mem, b->hv_features, b->hv_labels, b->hv_count, b->snap_body, b->snap_u8, b->body, b->awake, b->can_sleep, b->shape, b->d_bstart, b->d_bcount, b->d_ccap, b->d_ccount,
                  b->d_cstart, b->d_wstatus, b->d_piters, b->d_viters, b->contact, b->cbodies, b->work, b->wbodies,
                  b->d_order, b->d_order_rs, b->d_queue, b->d_status, b->d_counters, b->d_h2p, b->d_stage, b->d_stage_u8, b->d_stage_i32,
                  b->d_cstage, b->d_cstage_b, b->d_pow};
@@ -304,9 +317,9 @@ int configure(cz_batch* b) {
   // resolver shared-memory tile: shrink the contact capacity until it fits
   int cs = std::min<long long>(b->rs_cs, round_up(b->max_cap, 32));
   cs = std::max(cs, 32);
-  while (cs > 32 && b->ops->rs_smem(b->nbs, cs, b->rs_lanes) > b->smem_optin) cs -= 32;
+  while (cs > 32 && b->ops->rs_smem(b->nbs, cs, b->rs_lanes, b->mode) > b->smem_optin) cs -= 32;
   b->rs_cs = cs;
-  b->rs_smem = b->ops->rs_smem(b->nbs, cs, b->rs_lanes);
+  b->rs_smem = b->ops->rs_smem(b->nbs, cs, b->rs_lanes, b->mode);
   b->np_smem = b->ops->np_smem(b->nbs);
   if (b->np_smem > b->smem_optin || b->rs_smem > b->smem_optin)
     return fail(CZ_ERR_BODY_LIMIT, "world too large for the shared-memory tiles");
@@ -435,7 +448,7 @@ int cz_batch_create(const cz_batch_desc* d, cz_batch** out) {
   ok = ok && dmalloc(&b->contact, R * cz::C_NROWS * C) && dmalloc((void**)&b->cbodies, sizeof(int) * C);
   ok = ok && dmalloc(&b->work, R * cz::W_NROWS * C) && dmalloc((void**)&b->wbodies, sizeof(int) * C);
   ok = ok && dmalloc((void**)&b->d_queue, 4 * sizeof(unsigned)) && dmalloc((void**)&b->d_status, sizeof(uint32_t)) &&
-       dmalloc((void**)&b->d_counters, 4 * sizeof(unsigned long long));
+       dmalloc((void**)&b->d_counters, 8 * sizeof(unsigned long long));
   ok = ok && dmalloc((void**)&b->d_h2p, sizeof(int) * std::max<long long>(nb, 1));
   ok = ok && dmalloc((void**)&b->d_stage, sizeof(double) * cz::SG_NDOUBLES * std::max<long long>(nb, 1)) &&
        dmalloc((void**)&b->d_stage_u8, 2 * std::max<long long>(nb, 1)) &&
@@ -465,7 +478,7 @@ int cz_batch_create(const cz_batch_desc* d, cz_batch** out) {
       cudaMemsetAsync(b->d_viters, 0, sizeof(int) * W, s) != cudaSuccess ||
       cudaMemsetAsync(b->d_queue, 0, 4 * sizeof(unsigned), s) != cudaSuccess ||
       cudaMemsetAsync(b->d_status, 0, sizeof(uint32_t), s) != cudaSuccess ||
-      cudaMemsetAsync(b->d_counters, 0, 4 * sizeof(unsigned long long), s) != cudaSuccess ||
+      cudaMemsetAsync(b->d_counters, 0, 8 * sizeof(unsigned long long), s) != cudaSuccess ||
       cudaMemsetAsync(b->cbodies, 0xFF, sizeof(int) * C, s) != cudaSuccess ||
       cudaMemcpyAsync(b->d_bstart, b->bstart.data(), sizeof(int) * W, cudaMemcpyHostToDevice, s) != cudaSuccess ||
       cudaMemcpyAsync(b->d_bcount, bcount.data(), sizeof(int) * W, cudaMemcpyHostToDevice, s) != cudaSuccess ||
@@ -894,15 +907,92 @@ int cz_step_timed(cz_batch* b, int32_t nsteps, double dt, double* total_ms, doub
   return st;
 }
 
+int cz_set_warm_start(cz_batch* b, const float* blob) {
+  if (!b) return fail(CZ_ERR_BAD_ARG, "cz_set_warm_start: null batch");
+  CZ_CUDA(cudaSetDevice(b->device));
+  if (!blob) {
+    b->mode = 0;
+    return configure(b);
+  }
+  const size_t blob_bytes = sizeof(float) * cz::MLP_BLOB;
+  const size_t off = (blob_bytes + 255) & ~(size_t)255;
+  if (!b->mlp_mem) CZ_CUDA(cudaMalloc(&b->mlp_mem, off + cz::mlp_packed_bytes()));
+  unsigned char* mem = static_cast<unsigned char*>(b->mlp_mem);
+  CZ_CUDA(cudaMemcpyAsync(mem, blob, blob_bytes, cudaMemcpyHostToDevice, b->stream));
+  CZ_CUDA(cz::mlp_pack(reinterpret_cast<const float*>(mem), mem + off, b->stream));
+  CZ_CUDA(cudaStreamSynchronize(b->stream));
+  b->mlp = cz::mlp_view(mem + off);
+  b->mode = 2;
+  return configure(b);
+}
+
+int cz_harvest(cz_batch* b, int32_t nsteps, double dt, int32_t every, float* features, float* labels,
+               int64_t capacity, int64_t* count) {
+  if (!b || nsteps < 0 || every <= 0 || capacity < 0 || (capacity > 0 && (!features || !labels)))
+    return fail(CZ_ERR_BAD_ARG, "cz_harvest: bad argument");
+  CZ_CUDA(cudaSetDevice(b->device));
+  if (capacity > b->hv_cap) {
+    cudaFree(b->hv_features);
+    cudaFree(b->hv_labels);
+    b->hv_features = b->hv_labels = nullptr;
+    b->hv_cap = 0;
+    CZ_CUDA(cudaMalloc((void**)&b->hv_features, sizeof(float) * cz::MLP_IN * std::max<int64_t>(capacity, 1)));
+    CZ_CUDA(cudaMalloc((void**)&b->hv_labels, sizeof(float) * cz::MLP_OUT * std::max<int64_t>(capacity, 1)));
+    b->hv_cap = capacity;
+  }
+  if (!b->hv_count) CZ_CUDA(cudaMalloc((void**)&b->hv_count, sizeof(unsigned long long)));
+  CZ_CUDA(cudaMemsetAsync(b->hv_count, 0, sizeof(unsigned long long), b->stream));
+  int st = ensure_pows(b, dt);
+  if (st) return st;
+  if ((st = reset_status(b))) return st;
+  // the plain resolver, writing features and applied impulses every `every` frames
+  const int saved_mode = b->mode;
+  int cs = b->rs_cs;
+  while (cs > 32 && b->ops->rs_smem(b->nbs, cs, b->rs_lanes, 1) > b->smem_optin) cs -= 32;
+  const size_t smem1 = b->ops->rs_smem(b->nbs, cs, b->rs_lanes, 1);
+  CZ_CUDA(b->ops->prepare(b->np_smem, smem1, b->rs_lanes));
+  for (int s = 0; s < nsteps && st == CZ_OK; ++s) {
+    st = launch_integrate(b, dt);
+    if (!st) st = launch_narrowphase(b);
+    if (!st) {
+      const bool h = (s % every) == every - 1;
+      cz::HostView v = b->view();
+      v.mode = h ? 1 : 0;
+      v.hv_cap = b->hv_cap;
+      CZ_CUDA(cudaMemsetAsync(b->d_queue + 1, 0, sizeof(unsigned), b->stream));
+      CZ_CUDA(b->ops->resolve(v, b->nbs, h ? cs : b->rs_cs, b->rs_lanes, b->rs_grid, h ? smem1 : b->rs_smem, dt,
+                              b->stream));
+      g_launches++;
+      if (b->num_worlds > 32 / b->rs_lanes) {
+        k_reorder<<<1, 1024, 0, b->stream>>>(b->d_piters, b->d_viters, b->num_worlds, b->d_order_rs);
+        CZ_CUDA(cudaGetLastError());
+        g_launches++;
+      }
+    }
+  }
+  b->mode = saved_mode;
+  if (st) return st;
+  st = finish(b);
+  unsigned long long n = 0;
+  CZ_CUDA(cudaMemcpy(&n, b->hv_count, sizeof n, cudaMemcpyDeviceToHost));
+  const int64_t m = std::min<int64_t>((int64_t)n, capacity);
+  if (m > 0) {
+    CZ_CUDA(cudaMemcpy(features, b->hv_features, sizeof(float) * cz::MLP_IN * m, cudaMemcpyDeviceToHost));
+    CZ_CUDA(cudaMemcpy(labels, b->hv_labels, sizeof(float) * cz::MLP_OUT * m, cudaMemcpyDeviceToHost));
+  }
+  if (count) *count = m;
+  return st;
+}
+
 int cz_counters(cz_batch* b, int64_t* out, int32_t reset) {
   if (!b) return fail(CZ_ERR_BAD_ARG, "cz_counters: null batch");
   CZ_CUDA(cudaSetDevice(b->device));
-  unsigned long long c[4] = {0, 0, 0, 0};
+  unsigned long long c[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   CZ_CUDA(cudaMemcpyAsync(c, b->d_counters, sizeof c, cudaMemcpyDeviceToHost, b->stream));
   if (reset) CZ_CUDA(cudaMemsetAsync(b->d_counters, 0, sizeof c, b->stream));
   CZ_CUDA(cudaStreamSynchronize(b->stream));
   if (out)
-    for (int i = 0; i < 4; ++i) out[i] = (int64_t)c[i];
+    for (int i = 0; i < 6; ++i) out[i] = (int64_t)c[i];
   return CZ_OK;
 }
 

@@ -45,6 +45,12 @@ static BatchView<R> view_of(const HostView& h) {
   v.max_iterations = h.max_iterations;
   v.contact_writeback = h.contact_writeback;
   v.uniform_material = h.uniform_material;
+  v.mode = h.mode;
+  v.mlp = h.mlp;
+  v.hv_features = h.hv_features;
+  v.hv_labels = h.hv_labels;
+  v.hv_count = h.hv_count;
+  v.hv_cap = h.hv_cap;
   return v;
 }
 
@@ -155,25 +161,44 @@ __global__ void k_set_rows(BatchView<R> v, int row, int nrows, const double* __r
 }
 
 static size_t np_smem(int nbs) { return np_smem_bytes<R>(nbs); }
-static size_t rs_smem(int nbs, int cs, int lanes) { return (size_t)(32 / lanes) * rs_slot_bytes<R, W>(nbs, cs); }
+static size_t rs_smem(int nbs, int cs, int lanes, int mode) {
+  return (size_t)(32 / lanes) * rs_slot_bytes<R, W>(nbs, cs, mode) + (mode == 2 ? kMlpStageBytes : 0);
+}
 
-// the resolver instantiation for G lanes per world
-static const void* resolve_fn(int lanes) {
+// the resolver instantiation for G lanes per world, plain or with the
+// learned paths (harvest, warm start)
+static const void* resolve_fn_mode(int lanes, int mode) {
+  const bool learn = mode != 0;
   switch (lanes) {
-    case 4: return (const void*)k_resolve<R, W, 4>;
-    case 8: return (const void*)k_resolve<R, W, 8>;
-    case 16: return (const void*)k_resolve<R, W, 16>;
-    case 32: return (const void*)k_resolve<R, W, 32>;
+    case 4: return learn ? (const void*)k_resolve<R, W, 4, true> : (const void*)k_resolve<R, W, 4, false>;
+    case 8: return learn ? (const void*)k_resolve<R, W, 8, true> : (const void*)k_resolve<R, W, 8, false>;
+    case 16: return learn ? (const void*)k_resolve<R, W, 16, true> : (const void*)k_resolve<R, W, 16, false>;
+    case 32: return learn ? (const void*)k_resolve<R, W, 32, true> : (const void*)k_resolve<R, W, 32, false>;
     default: return nullptr;
   }
 }
+static const void* resolve_fn(int lanes) { return resolve_fn_mode(lanes, 0); }
+
+// Raise a kernel's dynamic shared-memory limit to `bytes` if it is lower.  The
+// limit is per function and process-wide, so it is never lowered: another
+// batch may launch the same kernel with a larger tile.
+static cudaError_t raise_smem_limit(const void* f, size_t bytes) {
+  cudaFuncAttributes a;
+  cudaError_t e = cudaFuncGetAttributes(&a, f);
+  if (e != cudaSuccess) return e;
+  if ((size_t)a.maxDynamicSharedSizeBytes >= bytes) return cudaSuccess;
+  return cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+}
 
 static cudaError_t prepare(size_t np, size_t rs, int lanes) {
-  cudaError_t e = cudaFuncSetAttribute(k_narrowphase<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)np);
+  cudaError_t e = raise_smem_limit((const void*)k_narrowphase<R>, np);
   if (e != cudaSuccess) return e;
-  const void* f = resolve_fn(lanes);
-  if (!f) return cudaErrorInvalidValue;
-  return cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rs);
+  for (int mode = 0; mode <= 1; ++mode) {
+    const void* f = resolve_fn_mode(lanes, mode);
+    if (!f) return cudaErrorInvalidValue;
+    if ((e = raise_smem_limit(f, rs)) != cudaSuccess) return e;
+  }
+  return cudaSuccess;
 }
 
 static cudaError_t integrate(const HostView& h, double dt, double bias, int threads, cudaStream_t s) {
@@ -191,13 +216,20 @@ static cudaError_t narrowphase(const HostView& h, int nbs, int threads, int grid
 static cudaError_t resolve(const HostView& h, int nbs, int cs, int lanes, int grid, size_t smem, double dt,
                            cudaStream_t s) {
   const BatchView<R> v = view_of(h);
+  const bool learn = h.mode != 0;
+#define CZ_LAUNCH_RS(G)                                                         \
+  if (learn)                                                                   \
+    k_resolve<R, W, G, true><<<grid, 32, smem, s>>>(v, nbs, cs, (R)dt);        \
+  else                                                                         \
+    k_resolve<R, W, G, false><<<grid, 32, smem, s>>>(v, nbs, cs, (R)dt);
   switch (lanes) {
-    case 4: k_resolve<R, W, 4><<<grid, 32, smem, s>>>(v, nbs, cs, (R)dt); break;
-    case 8: k_resolve<R, W, 8><<<grid, 32, smem, s>>>(v, nbs, cs, (R)dt); break;
-    case 16: k_resolve<R, W, 16><<<grid, 32, smem, s>>>(v, nbs, cs, (R)dt); break;
-    case 32: k_resolve<R, W, 32><<<grid, 32, smem, s>>>(v, nbs, cs, (R)dt); break;
+    case 4: CZ_LAUNCH_RS(4) break;
+    case 8: CZ_LAUNCH_RS(8) break;
+    case 16: CZ_LAUNCH_RS(16) break;
+    case 32: CZ_LAUNCH_RS(32) break;
     default: return cudaErrorInvalidValue;
   }
+#undef CZ_LAUNCH_RS
   return cudaGetLastError();
 }
 
@@ -218,7 +250,7 @@ static cudaError_t download(const HostView& h, double* sg, uint8_t* u8, int* i32
 static cudaError_t occupancy(int* npb, int np_threads, size_t nps, int* rsb, size_t rss, int lanes) {
   cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(npb, k_narrowphase<R>, np_threads, nps);
   if (e != cudaSuccess) return e;
-  const void* f = resolve_fn(lanes);
+  const void* f = resolve_fn(lanes);  // the plain kernel; the learned one has the same shared-memory use
   if (!f) return cudaErrorInvalidValue;
   return cudaOccupancyMaxActiveBlocksPerMultiprocessor(rsb, f, 32, rss);
 }

@@ -6,6 +6,8 @@
 #include <cstddef>
 #include <cstdint>
 
+#include "cz_mlp.cuh"
+
 namespace cz {
 
 // Type-erased device view; each form turns it into BatchView<R>.
@@ -40,6 +42,12 @@ struct HostView {
   int max_iterations;
   int contact_writeback;
   int uniform_material;
+  int mode;
+  MlpDev mlp;
+  float* hv_features;
+  float* hv_labels;
+  unsigned long long* hv_count;
+  long long hv_cap;
 };
 
 // Staging layout of host body data on the device (doubles, field blocks of n):
@@ -51,7 +59,7 @@ enum StageBlock : int {
 struct FormOps {
   size_t real_size;
   size_t (*np_smem)(int nbs);
-  size_t (*rs_smem)(int nbs, int cs, int lanes);  // per CTA (one warp, 32 / lanes worlds)
+  size_t (*rs_smem)(int nbs, int cs, int lanes, int mode);  // per CTA (one warp, 32 / lanes worlds)
   cudaError_t (*prepare)(size_t np_smem, size_t rs_smem, int lanes);  // function attributes
   cudaError_t (*integrate)(const HostView& v, double dt, double sleep_bias, int threads, cudaStream_t s);
   cudaError_t (*narrowphase)(const HostView& v, int nbs, int threads, int grid, size_t smem, cudaStream_t s);
@@ -74,6 +82,11 @@ struct FormOps {
 
 extern const FormOps kFormFP64;
 extern const FormOps kFormFP32;
+
+// Warm-start network: packed device copy of a float32 parameter blob.
+size_t mlp_packed_bytes();
+MlpDev mlp_view(unsigned char* packed);
+cudaError_t mlp_pack(const float* dev_blob, unsigned char* dev_packed, cudaStream_t s);
 
 // Records the message cz_last_error() returns; returns status.
 int set_error(int status, const char* what, cudaError_t e);

@@ -9,6 +9,8 @@
 #pragma once
 #include <cstdint>
 
+#include "cz_mlp.cuh"
+
 namespace cz {
 
 enum BodyRow : int {
@@ -40,8 +42,10 @@ enum WorkRow : int {
   W_R0X, W_R0Y, W_R0Z,
   W_R1X, W_R1Y, W_R1Z,
   W_CVX, W_CVY, W_CVZ,
+  W_J0, W_J1, W_J2,  // contact-frame impulse: predicted (warm start) or applied in total (harvest)
   W_NROWS
 };
+constexpr int W_NROWS_PLAIN = W_J0;  // rows the plain resolver keeps
 
 // World status bits (also OR-ed into the batch status word).
 enum : uint32_t {
@@ -92,12 +96,19 @@ template <class R> struct BatchView {
   unsigned* queue;      // [0] narrowphase, [1] resolver, [2..3] spare
   uint32_t* status;     // batch status word
   unsigned long long* counters;  // [0] contacts generated, [1] adjustPositions iterations,
-                                 // [2] adjustVelocities iterations, [3] contacts resolved
+                                 // [2] adjustVelocities iterations, [3] contacts resolved,
+                                 // [4] warm-started worlds re-solved plainly, [5] warm-started worlds
   R plane_nx, plane_ny, plane_nz, plane_offset;
   int iter_mult;        // ResolveContacts(len(contacts) * iter_mult)
   int max_iterations;   // >= 0 overrides len(contacts) * iter_mult
   int contact_writeback; // copy the resolved contacts back to the contact rows
   int uniform_material;  // every contact has the colliders' friction 0.9 / restitution 0.1
+  int mode;              // resolver: 0 plain, 1 harvest, 2 learned warm start
+  MlpDev mlp;            // warm-start network (mode 2)
+  float* hv_features;    // harvest output [hv_cap][18]
+  float* hv_labels;      // harvest output [hv_cap][3]
+  unsigned long long* hv_count;
+  long long hv_cap;
 };
 
 }  // namespace cz

@@ -17,6 +17,7 @@
 #pragma once
 #include "cz_layout.cuh"
 #include "cz_math.cuh"
+#include "cz_mlp.cuh"
 
 namespace cz {
 
@@ -29,6 +30,9 @@ template <class R, class W> struct RCtx {
   int* cb;        // packed bodies of this world's contacts
   long long cst;  // row stride of cw
   R* bc;          // broadcast scratch [12]
+  float* deg;     // [nbs] contacts touching each body (warm start / harvest)
+  R* save;        // [6][nbs] velocity and rotation before the warm start
+  R* delta;       // [6][nbs] warm-start velocity and rotation change per body
   const R* gmat;  // friction / restitution rows of the contact list (null: 0.9 / 0.1)
   long long gst;
   R dt;
@@ -332,7 +336,7 @@ __device__ v3<R> friction_impulse(const RCtx<R, W>& x, int k, int b0, int b1, co
 
 // applyVelocityChange, contact.go:447-494 (group leader); velocity and
 // rotation changes of both bodies go to x.bc[0..11].
-template <class R, class W>
+template <class R, class W, bool LEARN>
 __device__ void apply_velocity_change(const RCtx<R, W>& x, const BatchView<R>& v, int w, int k) {
   const int bb = x.cb[k];
   const int b0 = body0_of(bb), b1 = body1_of(bb);
@@ -353,6 +357,11 @@ __device__ void apply_velocity_change(const RCtx<R, W>& x, const BatchView<R>& v
   } else {
     ic = friction_impulse(x, k, b0, b1, C);
   }
+  if (LEARN && v.mode == 1) {  // harvest: total impulse applied at this contact
+    x.Cf(W_J0, k) += ic.x;
+    x.Cf(W_J0 + 1, k) += ic.y;
+    x.Cf(W_J0 + 2, k) += ic.z;
+  }
   const v3<R> imp = mulv(C, ic);
   const R z = (R)0;
   v3<R> vc0 = V<R>(z, z, z), vc1 = V<R>(z, z, z), rc1 = V<R>(z, z, z);
@@ -372,33 +381,259 @@ __device__ void apply_velocity_change(const RCtx<R, W>& x, const BatchView<R>& v
   x.bc[9] = rc1.x; x.bc[10] = rc1.y; x.bc[11] = rc1.z;
 }
 
-// Shared memory of one world's slot.
-template <class R, class W> __host__ __device__ inline size_t rs_slot_bytes(int nbs, int cs) {
+
+// ---------------------------------------------------------------- world slots
+// Shared memory of one world: body rows (W and R), contact working rows,
+// broadcast scratch, packed bodies, awake flags.  With the learned warm start
+// or harvesting (mode != 0) also the three impulse rows, per-body contact
+// degrees, the saved and delta velocities and two copies of the awake flags.
+template <class R, class W> __host__ __device__ inline size_t rs_slot_bytes(int nbs, int cs, int mode) {
+  const int rows = mode ? W_NROWS : W_NROWS_PLAIN;
+  const size_t nb16 = (size_t)((nbs + 15) & ~15);
   size_t b = (size_t)7 * nbs * sizeof(W);
   b += (size_t)20 * nbs * sizeof(R);
-  b += (size_t)W_NROWS * cs * sizeof(R);
+  b += (size_t)rows * cs * sizeof(R);
   b += 16 * sizeof(R);
+  if (mode) b += (size_t)13 * nbs * sizeof(R) + (size_t)nbs * sizeof(float);
   b += (size_t)cs * sizeof(int);
-  b += (size_t)((nbs + 15) & ~15);
+  b += nb16 * (mode ? 3 : 1);
   return (b + 15) & ~(size_t)15;
 }
+// staging of one 16-contact tile for the MLP (warm start only): BF16 inputs, FP32 outputs
+constexpr size_t kMlpStageBytes = 16 * MLP_K1 * 2 + 16 * 4 * 4;
 
+template <class R, class W> struct Slot {
+  RCtx<R, W> x;
+  R* cw_s;
+  int* cb_s;
+  uint8_t* aw_pos;  // awake flags at the start of adjustVelocities
+  uint8_t* aw_pre;  // awake flags at prepareContacts
+};
+
+template <class R, class W>
+__device__ __forceinline__ Slot<R, W> make_slot(unsigned char* base, int nbs, int cs, int mode, R dt) {
+  Slot<R, W> s;
+  RCtx<R, W>& x = s.x;
+  const int rows = mode ? W_NROWS : W_NROWS_PLAIN;
+  const int nb16 = (nbs + 15) & ~15;
+  x.nbs = nbs;
+  x.dt = dt;
+  x.bw = reinterpret_cast<W*>(base);
+  x.br = reinterpret_cast<R*>(x.bw + 7 * nbs);
+  s.cw_s = x.br + 20 * nbs;
+  x.bc = s.cw_s + (size_t)rows * cs;
+  R* after = x.bc + 16;
+  x.save = x.delta = nullptr;
+  x.deg = nullptr;
+  if (mode) {
+    x.save = after;            // [7][nbs]: vel 0-2, rot 3-5, motion 6
+    x.delta = after + 7 * nbs;  // [6][nbs]
+    x.deg = reinterpret_cast<float*>(after + 13 * nbs);
+    s.cb_s = reinterpret_cast<int*>(x.deg + nbs);
+  } else {
+    s.cb_s = reinterpret_cast<int*>(after);
+  }
+  x.aw = reinterpret_cast<uint8_t*>(s.cb_s + cs);
+  s.aw_pos = mode ? x.aw + nb16 : nullptr;
+  s.aw_pre = mode ? x.aw + 2 * nb16 : nullptr;
+  return s;
+}
+
+template <class R, class W>
+__device__ __forceinline__ void bind_contacts(Slot<R, W>& s, const BatchView<R>& v, int C, int cs, long long cst) {
+  RCtx<R, W>& x = s.x;
+  if (C <= cs) {
+    x.cw = s.cw_s;
+    x.cb = s.cb_s;
+    x.cst = cs;
+  } else {
+    x.cw = v.work + cst;
+    x.cb = v.work_bodies + cst;
+    x.cst = v.nc_total;
+  }
+  x.gmat = v.uniform_material ? nullptr : v.contact + (long long)C_FRIC * v.nc_total + cst;
+  x.gst = (long long)(C_REST - C_FRIC) * v.nc_total;
+}
+
+// The 18 features of a contact at the start of adjustVelocities: normal (3),
+// contact velocity in the contact basis (3), penetration, desired delta
+// velocity (restitution applied), the two inverse masses, the diagonal of
+// each body's world inverse inertia in the contact basis (3 + 3), and the
+// number of contacts touching each body (2).
+template <class R, class W> __device__ void contact_features(const RCtx<R, W>& x, int k, float* f) {
+  const int bb = x.cb[k];
+  const int b[2] = {body0_of(bb), body1_of(bb)};
+  const v3<R> n = x.Cv(W_NX, k), cv = x.Cv(W_CVX, k);
+  f[0] = (float)n.x; f[1] = (float)n.y; f[2] = (float)n.z;
+  f[3] = (float)cv.x; f[4] = (float)cv.y; f[5] = (float)cv.z;
+  f[6] = (float)x.Cf(W_PEN, k);
+  f[7] = (float)x.Cf(W_DDV, k);
+  const m3<R> C = x.basis(k);
+#pragma unroll
+  for (int i = 0; i < 2; ++i) {
+    f[8 + i] = b[i] >= 0 ? (float)x.Bf(18, b[i]) : 0.f;
+    f[16 + i] = b[i] >= 0 ? x.deg[b[i]] : 0.f;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      float d = 0.f;
+      if (b[i] >= 0) {
+        const v3<R> col = V<R>(C.m[3 * c], C.m[3 * c + 1], C.m[3 * c + 2]);
+        d = (float)dot(col, mulv(x.iit(b[i]), col));
+      }
+      f[10 + 3 * i + c] = d;
+    }
+  }
+}
+
+// The warm start of one world: every contact's predicted impulse applied at
+// once, bodies accumulating in contact order (deterministic), then every
+// contact's velocity and desired delta velocity brought up to date.  Every
+// lane of the warp calls it (it synchronises the warp); `on` selects the
+// groups whose world is being solved.
 template <class R, class W, int G>
+__device__ void apply_warm_start(const RCtx<R, W>& x, int n, int C, int gl, bool on) {
+  for (int i = gl; on && i < n; i += G) {
+    const R z = (R)0;
+    v3<R> dvel = V<R>(z, z, z), drot = V<R>(z, z, z);
+    const m3<R> I = x.iit(i);
+    const R invm = x.Bf(18, i);
+    for (int k = 0; k < C; ++k) {
+      const int bb = x.cb[k];
+      const int b0 = body0_of(bb), b1 = body1_of(bb);
+      if (b0 != i && b1 != i) continue;
+      const v3<R> J = x.Cv(W_J0, k);
+      const v3<R> imp = mulv(x.basis(k), J);
+      if (b0 == i) {
+        add(drot, mulv(I, cross(x.Cv(W_R0X, k), imp)));
+        add_scaled(dvel, imp, invm);
+      } else {
+        add(drot, mulv(I, cross(imp, x.Cv(W_R1X, k))));
+        add_scaled(dvel, imp, -invm);
+      }
+    }
+    // a body that receives nothing keeps its values bit for bit
+    const bool moved = dvel.x != z || dvel.y != z || dvel.z != z || drot.x != z || drot.y != z || drot.z != z;
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+      x.delta[r * x.nbs + i] = (&dvel.x)[r];
+      x.delta[(3 + r) * x.nbs + i] = (&drot.x)[r];
+      if (moved) {
+        x.Bf(r, i) += (&dvel.x)[r];
+        x.Bf(3 + r, i) += (&drot.x)[r];
+      }
+    }
+  }
+  __syncwarp();
+  // contacts touching a moved body: velocity and desired delta velocity as
+  // adjustVelocities updates them after an impulse (contact.go:416-445)
+  for (int k = gl; on && k < C; k += G) {
+    const int bb = x.cb[k];
+    const int kb[2] = {body0_of(bb), body1_of(bb)};
+    bool touched = false;
+#pragma unroll
+    for (int b = 0; b < 2; ++b) {
+      if (kb[b] < 0) continue;
+#pragma unroll
+      for (int r = 0; r < 6; ++r) touched |= x.delta[r * x.nbs + kb[b]] != (R)0;
+    }
+    if (!touched) continue;
+    const m3<R> Ck = x.basis(k);
+    v3<R> cv = x.Cv(W_CVX, k);
+#pragma unroll
+    for (int b = 0; b < 2; ++b) {
+      const int body = kb[b];
+      if (body < 0) continue;
+      const v3<R> r = b == 0 ? x.Cv(W_R0X, k) : x.Cv(W_R1X, k);
+      const v3<R> dr = V<R>(x.delta[3 * x.nbs + body], x.delta[4 * x.nbs + body], x.delta[5 * x.nbs + body]);
+      const v3<R> dl = V<R>(x.delta[body], x.delta[x.nbs + body], x.delta[2 * x.nbs + body]);
+      v3<R> dv = cross(dr, r);
+      add(dv, dl);
+      v3<R> t = mulv_t(Ck, dv);
+      mul_with(t, b == 1 ? (R)-1 : (R)1);
+      add(cv, t);
+    }
+    x.setCv(W_CVX, k, cv);
+    x.Cf(W_DDV, k) = desired_dv(x, k);
+  }
+}
+
+// adjustVelocities, contact.go:388-445, for the groups with run set; returns
+// the iterations used.
+template <class R, class W, int G, bool LEARN>
+__device__ int velocity_loop(const RCtx<R, W>& x, const BatchView<R>& v, int w, int C, int gl, int max_it, bool run) {
+  int used = 0;
+  while (__any_sync(FULL, run)) {
+    auto best = key_of((R)0, (R)0);
+    int bidx = 0x7fffffff;
+    if (run) {
+      for (int k = gl; k < C; k += G) {
+        const auto key = key_of(x.Cf(W_DDV, k), (R)0.01);
+        if (key > best) {
+          best = key;
+          bidx = k;
+        }
+      }
+    }
+    group_first_max<G>(best, bidx);
+    if (best == 0) run = false;
+    if (run && gl == 0) {
+      match_awake(x, x.cb[bidx]);
+      apply_velocity_change<R, W, LEARN>(x, v, w, bidx);
+    }
+    __syncwarp();
+    if (run) {
+      const int rb = x.cb[bidx];
+      const int d0 = body0_of(rb), d1 = body1_of(rb);
+      for (int k = gl; k < C; k += G) {
+        const int bb = x.cb[k];
+        const int kb[2] = {body0_of(bb), body1_of(bb)};
+        const bool m0 = kb[0] == d0 || (d1 >= 0 && kb[0] == d1);
+        const bool m1 = kb[1] >= 0 && (kb[1] == d0 || kb[1] == d1);
+        if (!m0 && !m1) continue;
+        const m3<R> Ck = x.basis(k);
+        v3<R> cv = x.Cv(W_CVX, k);
+#pragma unroll
+        for (int b = 0; b < 2; ++b) {
+          if (kb[b] < 0) continue;
+          const v3<R> r = b == 0 ? x.Cv(W_R0X, k) : x.Cv(W_R1X, k);
+#pragma unroll
+          for (int d = 0; d < 2; ++d) {
+            if (kb[b] == (d == 0 ? d0 : d1)) {
+              v3<R> dv = cross(V<R>(x.bc[6 + 3 * d], x.bc[7 + 3 * d], x.bc[8 + 3 * d]), r);
+              add(dv, V<R>(x.bc[3 * d], x.bc[3 * d + 1], x.bc[3 * d + 2]));
+              const R sign = b == 1 ? (R)-1 : (R)1;
+              v3<R> t = mulv_t(Ck, dv);
+              mul_with(t, sign);
+              add(cv, t);
+            }
+          }
+        }
+        x.setCv(W_CVX, k, cv);
+        x.Cf(W_DDV, k) = desired_dv(x, k);
+      }
+    }
+    __syncwarp();
+    if (run && ++used >= max_it) run = false;
+  }
+  return used;
+}
+
+// v.mode: 0 plain, 1 harvest (plain, writing features and applied impulses),
+// 2 learned warm start with fallback to the plain solve.  LEARN = false
+// compiles the plain resolver alone (v.mode is ignored), so the learned
+// paths cost the plain kernel no registers.
+template <class R, class W, int G, bool LEARN>
 __global__ void __launch_bounds__(32) k_resolve(BatchView<R> v, int nbs, int cs, R dt) {
   constexpr int NG = 32 / G;
   extern __shared__ __align__(128) unsigned char smem[];
   const int lane = threadIdx.x;
   const int grp = lane / G, gl = lane % G;
-  unsigned char* base = smem + (size_t)grp * rs_slot_bytes<R, W>(nbs, cs);
-  RCtx<R, W> x;
-  x.nbs = nbs;
-  x.dt = dt;
-  x.bw = reinterpret_cast<W*>(base);
-  x.br = reinterpret_cast<R*>(x.bw + 7 * nbs);
-  R* cw_s = x.br + 20 * nbs;
-  x.bc = cw_s + (size_t)W_NROWS * cs;
-  int* cb_s = reinterpret_cast<int*>(x.bc + 16);
-  x.aw = reinterpret_cast<uint8_t*>(cb_s + cs);
+  const int mode = LEARN ? v.mode : 0;
+  const size_t slot_bytes = rs_slot_bytes<R, W>(nbs, cs, mode);
+  Slot<R, W> sl = make_slot<R, W>(smem + (size_t)grp * slot_bytes, nbs, cs, mode, dt);
+  RCtx<R, W>& x = sl.x;
+  __nv_bfloat16* stage_in = reinterpret_cast<__nv_bfloat16*>(smem + (size_t)NG * slot_bytes);
+  float* stage_out = reinterpret_cast<float*>(stage_in + 16 * MLP_K1);
   const long long S = v.nb_pad;
   for (;;) {
     unsigned q0 = 0;
@@ -428,17 +663,7 @@ __global__ void __launch_bounds__(32) k_resolve(BatchView<R> v, int nbs, int cs,
       active = false;
     }
     const long long cst = has ? v.contact_start[w] : 0;
-    if (C <= cs) {
-      x.cw = cw_s;
-      x.cb = cb_s;
-      x.cst = cs;
-    } else {
-      x.cw = v.work + cst;
-      x.cb = v.work_bodies + cst;
-      x.cst = v.nc_total;
-    }
-    x.gmat = v.uniform_material ? nullptr : v.contact + (long long)C_FRIC * v.nc_total + cst;
-    x.gst = (long long)(C_REST - C_FRIC) * v.nc_total;
+    bind_contacts(sl, v, C, cs, cst);
     if (active) {
       for (int i = gl; i < n; i += G) {
         const long long g = bstart + i;
@@ -460,6 +685,7 @@ __global__ void __launch_bounds__(32) k_resolve(BatchView<R> v, int nbs, int cs,
         x.Bf(18, i) = v.body[B_INVM * S + g];
         x.Bf(19, i) = v.body[B_MOTION * S + g];
         x.aw[i] = v.awake[g];
+        if (mode) sl.aw_pre[i] = x.aw[i];
       }
     }
     __syncwarp();
@@ -498,7 +724,7 @@ __global__ void __launch_bounds__(32) k_resolve(BatchView<R> v, int nbs, int cs,
           const bool m0 = kb[0] == d0 || (d1 >= 0 && kb[0] == d1);
           const bool m1 = kb[1] >= 0 && (kb[1] == d0 || kb[1] == d1);
           if (!m0 && !m1) continue;
-          const v3<R> n = x.Cv(W_NX, k);
+          const v3<R> nk = x.Cv(W_NX, k);
           R pen = x.Cf(W_PEN, k);
 #pragma unroll
           for (int b = 0; b < 2; ++b) {
@@ -510,7 +736,7 @@ __global__ void __launch_bounds__(32) k_resolve(BatchView<R> v, int nbs, int cs,
                 v3<R> dp = cross(V<R>(x.bc[6 + 3 * d], x.bc[7 + 3 * d], x.bc[8 + 3 * d]), r);
                 add(dp, V<R>(x.bc[3 * d], x.bc[3 * d + 1], x.bc[3 * d + 2]));
                 const R sign = b == 0 ? (R)-1 : (R)1;
-                pen += dot(dp, n) * sign;
+                pen += dot(dp, nk) * sign;
               }
             }
           }
@@ -521,67 +747,139 @@ __global__ void __launch_bounds__(32) k_resolve(BatchView<R> v, int nbs, int cs,
       if (run && ++used >= max_it) run = false;
     }
     const int pos_used = used;
-    // ---------------- adjustVelocities, contact.go:388-445
-    used = 0;
-    run = active && max_it > 0;
-    while (__any_sync(FULL, run)) {
-      auto best = key_of((R)0, (R)0);
-      int bidx = 0x7fffffff;
-      if (run) {
-        for (int k = gl; k < C; k += G) {
-          const auto key = key_of(x.Cf(W_DDV, k), (R)0.01);
-          if (key > best) {
-            best = key;
-            bidx = k;
-          }
-        }
-      }
-      group_first_max<G>(best, bidx);
-      if (best == 0) run = false;
-      if (run && gl == 0) {
-        match_awake(x, x.cb[bidx]);
-        apply_velocity_change(x, v, w, bidx);
-      }
-      __syncwarp();
-      if (run) {
-        const int rb = x.cb[bidx];
-        const int d0 = body0_of(rb), d1 = body1_of(rb);
-        for (int k = gl; k < C; k += G) {
+    // ---------------- learned warm start / harvest set-up
+    const bool solve = active && max_it > 0;
+    long long hv_base = -1;
+    if (LEARN && mode && solve) {
+      for (int i = gl; i < n; i += G) {
+        int d = 0;
+        for (int k = 0; k < C; ++k) {
           const int bb = x.cb[k];
-          const int kb[2] = {body0_of(bb), body1_of(bb)};
-          const bool m0 = kb[0] == d0 || (d1 >= 0 && kb[0] == d1);
-          const bool m1 = kb[1] >= 0 && (kb[1] == d0 || kb[1] == d1);
-          if (!m0 && !m1) continue;
-          const m3<R> Ck = x.basis(k);
-          v3<R> cv = x.Cv(W_CVX, k);
+          d += (body0_of(bb) == i) + (body1_of(bb) == i);
+        }
+        x.deg[i] = (float)d;
+        sl.aw_pos[i] = x.aw[i];
 #pragma unroll
-          for (int b = 0; b < 2; ++b) {
-            if (kb[b] < 0) continue;
-            const v3<R> r = b == 0 ? x.Cv(W_R0X, k) : x.Cv(W_R1X, k);
+        for (int r = 0; r < 6; ++r) x.save[r * nbs + i] = x.Bf(r, i);
+        x.save[6 * nbs + i] = x.Bf(19, i);
+      }
+      for (int k = gl; k < C; k += G) {
+        x.Cf(W_J0, k) = (R)0;
+        x.Cf(W_J0 + 1, k) = (R)0;
+        x.Cf(W_J0 + 2, k) = (R)0;
+      }
+    }
+    __syncwarp();
+    if (LEARN && mode == 1) {
+      // every lane takes part in the shuffle; only solving groups reserve rows
+      unsigned long long b0 = 0;
+      if (solve && gl == 0) b0 = atomicAdd(v.hv_count, (unsigned long long)C);
+      b0 = __shfl_sync(FULL, b0, grp * G);
+      if (solve && (long long)(b0 + C) <= v.hv_cap) {
+        hv_base = (long long)b0;
+        for (int k = gl; k < C; k += G) contact_features(x, k, v.hv_features + (hv_base + k) * MLP_IN);
+      }
+    }
+    if (LEARN && mode == 2) {
+      // inference, one 16-contact tile at a time, over the worlds of this warp
+      for (int gi = 0; gi < NG; ++gi) {
+        const int Cg = __shfl_sync(FULL, solve ? C : 0, gi * G);
+        const long long cstg = __shfl_sync(FULL, cst, gi * G);
+        if (Cg == 0) continue;
+        Slot<R, W> sg = make_slot<R, W>(smem + (size_t)gi * slot_bytes, nbs, cs, mode, dt);
+        bind_contacts(sg, v, Cg, cs, cstg);
+        for (int t0 = 0; t0 < Cg; t0 += 16) {
+          if (lane < 16) {
+            const int k = t0 + lane;
+            float f[MLP_IN];
+            if (k < Cg) contact_features(sg.x, k, f);
 #pragma unroll
-            for (int d = 0; d < 2; ++d) {
-              if (kb[b] == (d == 0 ? d0 : d1)) {
-                v3<R> dv = cross(V<R>(x.bc[6 + 3 * d], x.bc[7 + 3 * d], x.bc[8 + 3 * d]), r);
-                add(dv, V<R>(x.bc[3 * d], x.bc[3 * d + 1], x.bc[3 * d + 2]));
-                const R sign = b == 1 ? (R)-1 : (R)1;
-                v3<R> t = mulv_t(Ck, dv);
-                mul_with(t, sign);
-                add(cv, t);
-              }
+            for (int c = 0; c < MLP_K1; c += 2) {
+              float lo = 0.f, hi = 0.f;
+              if (k < Cg && c < MLP_IN) lo = (f[c] - v.mlp.mu[c]) * v.mlp.inv_sigma[c];
+              if (k < Cg && c + 1 < MLP_IN) hi = (f[c + 1] - v.mlp.mu[c + 1]) * v.mlp.inv_sigma[c + 1];
+              *reinterpret_cast<unsigned*>(stage_in + lane * MLP_K1 + c) = pack_bf16(lo, hi);
             }
           }
-          x.setCv(W_CVX, k, cv);
-          x.Cf(W_DDV, k) = desired_dv(x, k);
+          __syncwarp();
+          unsigned a[2][4];
+          load_a<2>(stage_in, MLP_K1, a);
+          float o[4];
+          mlp_forward_tile(v.mlp, a, o);
+          const int g = lane >> 2, t = lane & 3;
+          if (t < 2) {
+            stage_out[g * 4 + 2 * t] = o[0];
+            stage_out[(g + 8) * 4 + 2 * t] = o[2];
+            if (t == 0) {
+              stage_out[g * 4 + 1] = o[1];
+              stage_out[(g + 8) * 4 + 1] = o[3];
+            }
+          }
+          __syncwarp();
+          if (lane < 16 && t0 + lane < Cg) {
+#pragma unroll
+            for (int c = 0; c < 3; ++c) sg.x.Cf(W_J0 + c, t0 + lane) = (R)(stage_out[lane * 4 + c] * v.mlp.out_scale[c]);
+          }
+          __syncwarp();
         }
       }
+      apply_warm_start<R, W, G>(x, n, C, gl, solve);
       __syncwarp();
-      if (run && ++used >= max_it) run = false;
+    }
+    // ---------------- adjustVelocities, contact.go:388-445
+    used = velocity_loop<R, W, G, LEARN>(x, v, w, C, gl, max_it, solve);
+    int vel_used = used;
+    if (LEARN && mode == 2) {
+      // the plain resolver stays the judge: a world that used all its
+      // iterations is solved again by the plain path from the saved state
+      const bool fb = solve && used >= max_it;
+      if (__any_sync(FULL, fb)) {
+        if (fb) {
+          for (int i = gl; i < n; i += G) {
+#pragma unroll
+            for (int r = 0; r < 6; ++r) x.Bf(r, i) = x.save[r * nbs + i];
+            x.Bf(19, i) = x.save[6 * nbs + i];
+            x.aw[i] = sl.aw_pos[i];
+          }
+        }
+        __syncwarp();
+        if (fb) {
+          // contact velocities as prepareContacts left them (same velocities,
+          // relative positions and basis), desired delta velocity with the
+          // awake flags of that moment
+          uint8_t* aw_now = x.aw;
+          x.aw = sl.aw_pre;
+          for (int k = gl; k < C; k += G) {
+            const int bb = x.cb[k];
+            const int b0 = body0_of(bb), b1 = body1_of(bb);
+            const m3<R> Ck = x.basis(k);
+            v3<R> cv = local_velocity(x, b0, x.Cv(W_R0X, k), Ck);
+            if (b1 >= 0) sub(cv, local_velocity(x, b1, x.Cv(W_R1X, k), Ck));
+            x.setCv(W_CVX, k, cv);
+            x.Cf(W_DDV, k) = desired_dv(x, k);
+          }
+          x.aw = aw_now;
+        }
+        __syncwarp();
+        const int used2 = velocity_loop<R, W, G, LEARN>(x, v, w, C, gl, max_it, fb);
+        if (fb) vel_used += used2;
+        if (fb && gl == 0) atomicAdd(&v.counters[4], 1ull);
+      }
+      if (solve && gl == 0) atomicAdd(&v.counters[5], 1ull);
+    }
+    if (LEARN && mode == 1 && hv_base >= 0) {
+      for (int k = gl; k < C; k += G) {
+        float* lab = v.hv_labels + (hv_base + k) * MLP_OUT;
+        lab[0] = (float)x.Cf(W_J0, k);
+        lab[1] = (float)x.Cf(W_J0 + 1, k);
+        lab[2] = (float)x.Cf(W_J0 + 2, k);
+      }
     }
     if (has && gl == 0) {
       v.pos_iters[w] = pos_used;
-      v.vel_iters[w] = used;
+      v.vel_iters[w] = vel_used;
       atomicAdd(&v.counters[1], (unsigned long long)pos_used);
-      atomicAdd(&v.counters[2], (unsigned long long)used);
+      atomicAdd(&v.counters[2], (unsigned long long)vel_used);
       atomicAdd(&v.counters[3], (unsigned long long)C);
     }
     if (active && v.contact_writeback) {

@@ -54,7 +54,7 @@ static __device__ __align__(256) unsigned char g_static_scratch[kScratchBytes];
 // counters and per-world metadata of the single world, inside the scratch
 struct Meta {
   long long contact_start;
-  unsigned long long counters[4];
+  unsigned long long counters[8];
   int body_start, body_count, contact_cap, contact_count;
   uint32_t world_status, status;
   int pos_iters, vel_iters, order, order_rs;
@@ -124,10 +124,8 @@ __global__ void k_static_in(unsigned char* scratch, cz_bodies in, const cz_conta
 __global__ void k_static_reset(unsigned char* scratch, int n, int nc) {
   Meta* m = reinterpret_cast<Meta*>(scratch + kOffMeta);
   m->contact_start = 0;
-  for (int i = 0; i < 4; ++i) {
-    m->counters[i] = 0;
-    m->queue[i] = 0;
-  }
+  for (int i = 0; i < 8; ++i) m->counters[i] = 0;
+  for (int i = 0; i < 4; ++i) m->queue[i] = 0;
   m->body_start = 0;
   m->body_count = n;
   m->contact_cap = nc;
@@ -231,6 +229,7 @@ cz::HostView static_view(unsigned char* scratch, int n) {
   v.max_iterations = 0;
   v.contact_writeback = 1;
   v.uniform_material = 0;
+  v.mode = 0;
   return v;
 }
 
@@ -253,7 +252,7 @@ int resolve_static(const cz::FormOps& ops, int32_t max_iterations, cz_contact* c
     return cz::set_error(CZ_ERR_CUDA, "cz_resolve_contacts_static: input kernels", e);
   cz::HostView v = static_view<R>(scratch, n);
   v.max_iterations = max_iterations < 0 ? 0 : max_iterations;
-  const size_t smem = ops.rs_smem(kStaticMaxBodies, kStaticContactTile, 32);
+  const size_t smem = ops.rs_smem(kStaticMaxBodies, kStaticContactTile, 32, 0);
   // the kernel's dynamic shared-memory limit may have been set by a batch:
   // raise it when this launch needs more, never lower it
   const void* fn = ops.resolve_kernel(32);

@@ -1,0 +1,116 @@
+"""The learned warm start of adjustVelocities (host side).
+
+  harvest(batch, ...)   features and total applied contact-frame impulses of
+                        the plain resolver (the training set)
+  Trainer               the GPU trainer (hand-written BF16 tensor-core
+                        forward/backward kernels, Adam on FP32 masters)
+  batch.set_warm_start  enable the network inside the resolver
+
+The network: 18 features -> 64 -> 64 -> 64 -> 3, ReLU.  Parameter blobs are
+float32 arrays of BLOB floats in the layout of include/cubez_gpu.h.
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from ._lib import check
+
+IN, H, OUT = 18, 64, 3
+OFF_W1 = 0
+OFF_B1 = OFF_W1 + H * IN
+OFF_W2 = OFF_B1 + H
+OFF_B2 = OFF_W2 + H * H
+OFF_W3 = OFF_B2 + H
+OFF_B3 = OFF_W3 + H * H
+OFF_W4 = OFF_B3 + H
+OFF_B4 = OFF_W4 + OUT * H
+NPARAM = OFF_B4 + OUT
+OFF_MU = NPARAM
+OFF_IS = OFF_MU + IN
+OFF_OS = OFF_IS + IN
+BLOB = OFF_OS + OUT
+
+FEATURES = ("normal_x", "normal_y", "normal_z", "cv_x", "cv_y", "cv_z", "penetration", "desired_dv",
+            "inv_mass_0", "inv_mass_1", "iw0_nn", "iw0_yy", "iw0_zz", "iw1_nn", "iw1_yy", "iw1_zz",
+            "contacts_body_0", "contacts_body_1")
+
+
+def _ptr(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def lib():
+    return _lib.load()
+
+
+def harvest(batch, nsteps, dt=1.0 / 60.0, every=10, capacity=1 << 20):
+    """Step `batch` nsteps frames with the plain resolver; every `every`
+    frames record each contact's features and the impulse adjustVelocities
+    applied to it in total.  Returns (features [n,18], labels [n,3])."""
+    L = lib()
+    f = np.zeros((capacity, IN), np.float32)
+    y = np.zeros((capacity, OUT), np.float32)
+    n = C.c_int64(0)
+    check(L.cz_harvest(batch.h, int(nsteps), float(dt), int(every), _ptr(f), _ptr(y), int(capacity), C.byref(n)))
+    return f[:n.value].copy(), y[:n.value].copy()
+
+
+def set_warm_start(batch, blob):
+    """Enable the warm start with a parameter blob, or disable it (None)."""
+    L = lib()
+    if blob is None:
+        check(L.cz_set_warm_start(batch.h, None))
+    else:
+        b = np.ascontiguousarray(blob, np.float32)
+        assert b.shape == (BLOB,)
+        check(L.cz_set_warm_start(batch.h, _ptr(b)))
+
+
+class Trainer:
+    """GPU trainer of the warm-start network (cz_mlp_*)."""
+
+    def __init__(self, seed=0, device=0):
+        self.L = lib()
+        h = C.c_void_p()
+        check(self.L.cz_mlp_create(device, seed, C.byref(h)))
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.cz_mlp_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def params(self):
+        b = np.zeros(BLOB, np.float32)
+        check(self.L.cz_mlp_get_params(self.h, _ptr(b)))
+        return b
+
+    def set_params(self, blob):
+        b = np.ascontiguousarray(blob, np.float32)
+        check(self.L.cz_mlp_set_params(self.h, _ptr(b)))
+
+    def set_data(self, x, y, normalize=True):
+        self._x = np.ascontiguousarray(x, np.float32)
+        self._y = np.ascontiguousarray(y, np.float32)
+        check(self.L.cz_mlp_set_data(self.h, _ptr(self._x), _ptr(self._y), len(self._x), 1 if normalize else 0))
+
+    def train(self, epochs, batch=4096, lr=1e-3, seed=1):
+        losses = np.zeros(epochs, np.float32)
+        check(self.L.cz_mlp_train(self.h, int(epochs), int(batch), float(lr), int(seed), _ptr(losses)))
+        return losses
+
+    def loss_and_grad(self, n):
+        loss = C.c_float(0.0)
+        g = np.zeros(NPARAM, np.float32)
+        check(self.L.cz_mlp_loss_and_grad(self.h, int(n), C.byref(loss), _ptr(g)))
+        return loss.value, g
+
+    def predict(self, x):
+        x = np.ascontiguousarray(x, np.float32)
+        out = np.zeros((len(x), OUT), np.float32)
+        check(self.L.cz_mlp_predict(self.h, _ptr(x), len(x), _ptr(out)))
+        return out

@@ -158,9 +158,11 @@ int cz_restore(cz_batch* batch);
 int cz_step_timed(cz_batch* batch, int32_t nsteps, double dt, double* total_ms, double* phase_ms);
 
 /* Running totals since creation or the last reset: [0] contacts generated,
- * [1] adjustPositions iterations, [2] adjustVelocities iterations, [3]
- * contacts resolved.  reset != 0 zeroes them after reading. */
-int cz_counters(cz_batch* batch, int64_t* out /* [4] */, int32_t reset);
+ * [1] adjustPositions iterations, [2] adjustVelocities iterations (with the
+ * warm start: both solves of a re-solved world), [3] contacts resolved,
+ * [4] warm-started worlds re-solved by the plain path, [5] warm-started
+ * worlds.  reset != 0 zeroes them after reading. */
+int cz_counters(cz_batch* batch, int64_t* out /* [6] */, int32_t reset);
 
 /* Sizes: [0] bodies, [1] padded bodies, [2] contact slots, [3] bytes per real,
  * [4] SMs, [5] narrowphase CTAs, [6] resolver CTAs, [7] narrowphase shared
@@ -187,6 +189,49 @@ int cz_batch_info(cz_batch* batch, int64_t* info /* [9] */);
  *   work overlaps race on it: serialise them. */
 int cz_resolve_contacts_static(int32_t form, int32_t max_iterations, cz_contact* contacts, int32_t ncontacts,
                                double duration, const cz_bodies* bodies, int32_t nbodies, void* stream);
+
+/* ---- Learned warm start of adjustVelocities (no counterpart in the
+ * reference; the precision form's third variant).  A parameter blob is
+ * CZ_MLP_BLOB floats: W1[64][18] b1[64] W2[64][64] b2[64] W3[64][64] b3[64]
+ * W4[3][64] b4[3] (trainable), then the feature mean[18], 1/std[18] and the
+ * output scale[3].  The network maps 18 contact features (normal, contact
+ * velocity in the contact basis, penetration, desired delta velocity, the
+ * two inverse masses, each body's world inverse inertia diagonal in the
+ * contact basis, the contacts touching each body) to the contact-frame
+ * impulse the plain resolver applies in total; the predictions are applied
+ * before adjustVelocities, which then runs to the reference's epsilons; a
+ * world that uses all its iterations is re-solved by the plain path. */
+#define CZ_MLP_IN 18
+#define CZ_MLP_OUT 3
+#define CZ_MLP_NPARAM 9539
+#define CZ_MLP_BLOB 9578
+
+/* Enable the warm start with a parameter blob (host floats), or disable it
+ * (blob = NULL).  Affects cz_step / cz_step_timed / cz_resolve. */
+int cz_set_warm_start(cz_batch* batch, const float* blob);
+
+/* Run nsteps frames with the plain resolver and, every `every` frames, write
+ * each contact's features and the contact-frame impulse adjustVelocities
+ * applied to it in total (the training labels) to host arrays
+ * features[capacity][18], labels[capacity][3]; *count = rows written. */
+int cz_harvest(cz_batch* batch, int32_t nsteps, double dt, int32_t every, float* features, float* labels,
+               int64_t capacity, int64_t* count);
+
+/* Trainer of the warm-start network: hand-written BF16 tensor-core forward,
+ * backward and weight-gradient kernels with FP32 accumulation, Adam on FP32
+ * master weights, mean squared error on normalised outputs. */
+typedef struct cz_mlp cz_mlp;
+int cz_mlp_create(int32_t device, uint64_t seed, cz_mlp** out);
+int cz_mlp_destroy(cz_mlp* mlp);
+int cz_mlp_get_params(cz_mlp* mlp, float* blob /* [CZ_MLP_BLOB] */);
+int cz_mlp_set_params(cz_mlp* mlp, const float* blob);
+/* Training data (host arrays, copied); set_normalization != 0 also sets the
+ * feature mean / std and output scale from the data. */
+int cz_mlp_set_data(cz_mlp* mlp, const float* features, const float* labels, int64_t n, int32_t set_normalization);
+int cz_mlp_train(cz_mlp* mlp, int32_t epochs, int32_t batch, float lr, uint64_t seed, float* epoch_loss);
+/* Mean loss and gradient over the first n data rows, without an update. */
+int cz_mlp_loss_and_grad(cz_mlp* mlp, int64_t n, float* loss, float* grad /* [CZ_MLP_NPARAM] */);
+int cz_mlp_predict(cz_mlp* mlp, const float* features, int64_t n, float* impulses /* [n][3] */);
 
 /* Tuning knobs picked by the autotuner (0 keeps the current value). */
 typedef struct cz_tuning {

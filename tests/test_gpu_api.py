@@ -150,6 +150,21 @@ def test_bad_arguments_on_a_live_batch(cuda_lib):
     assert b.L.cz_resolve_contacts(b.h, 4, C.cast(arr, C.c_void_p), 1, DT, C.byref(s)) == 1
 
 
+def test_batches_with_different_tiles_coexist(cuda_lib):
+    """A kernel's shared-memory limit is process-wide: a batch with a small
+    tile created later must not stop an earlier batch with a large tile."""
+    from cubez_gb300.batch import WorldBatch
+    scene = scenes.mixed(num_worlds=16, seed=34)
+    big = WorldBatch.from_scene(scene)
+    big.set_tuning(resolver_lanes=8, resolver_contacts=256)
+    small = WorldBatch.from_scene(scene)
+    small.set_tuning(resolver_lanes=8, resolver_contacts=32)
+    big.step(5, DT)
+    small.step(5, DT)
+    a, b = big.download(), small.download()
+    np.testing.assert_array_equal(a["position"], b["position"])
+
+
 def test_kernel_launch_accounting(cuda_lib):
     from cubez_gb300 import _lib
     from cubez_gb300.batch import WorldBatch
