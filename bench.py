@@ -10,12 +10,16 @@ One benchmark "step" is one 600-frame rollout of all worlds from the same
 initial state, captured as one CUDA graph (integrate -> narrowphase -> resolve
 per frame).  The metric is body-steps/s = bodies x frames / time.
 
-  value       precision form (float32 bulk, float64 islands), device time of
-              the rollout graph (CUDA events recorded on the batch stream inside
-              the graph), inputs resident in HBM
+  value       precision form (float32 bulk, float64 islands) with the learned
+              warm start of adjustVelocities (network trained before timing,
+              on the GPU, on contacts harvested from scenes of other seeds),
+              device time of the rollout graph (CUDA events recorded on the
+              batch stream inside the graph), inputs resident in HBM
   e2e         the same through the C ABI with host buffers: cz_upload_bodies
               (host -> device) + cz_step + cz_download_bodies (device -> host)
+  fp32_plain  the precision form without the warm start, measured the same way
   fp64        the plain float64 form measured the same way (reported beside it)
+  accuracy    both precision variants against the float64 form
   roofline    the dominant kernel, algorithmic bytes per launch / its average
               CUDA-event duration over the timed rollouts
   cpu_baseline  the oracle (C++ restatement of the reference's float64 Go path)
@@ -134,24 +138,16 @@ def _kinetic_energy(d, scene):
     return lin + ang
 
 
-def accuracy(scene, frames, batches):
-    """Errors of the precision form against the plain float64 form (bit-exact
-    with the oracle) on identical initial states: one-step relative error per
-    quantity, time-averaged kinetic energy and final mean height."""
-    out = {}
+def accuracy(scene, frames, batches, forms=("fp32_mlp", "fp32")):
+    """Errors of the precision variants against the plain float64 form
+    (bit-exact with the oracle) on identical initial states: one-step
+    relative error per quantity (per body, max-norm error over max(|value|, 1)),
+    time-averaged kinetic energy and final mean height."""
     res = {}
     for name, b in batches.items():
         b.restore()
         b.step(1, DT)
         res[name] = b.download()
-    a, r = res["fp32"], res["fp64"]
-    floors = {"position": 1.0, "orientation": 1.0, "velocity": 1.0, "rotation": 1.0}
-    one = {}
-    for k, fl in floors.items():
-        den = np.maximum(np.abs(r[k]).max(axis=1), fl)
-        e = np.abs(a[k] - r[k]).max(axis=1) / den
-        one[k] = {"max": float(e.max()), "p99": float(np.quantile(e, 0.99))}
-    out["one_step_rel_error"] = one
     ke = {name: [] for name in batches}
     height = {}
     seg = 30
@@ -162,10 +158,21 @@ def accuracy(scene, frames, batches):
             d = b.download()
             ke[name].append(float(_kinetic_energy(d, scene).sum()))
         height[name] = float(d["position"][:, 1].mean())
-    ke32, ke64 = np.mean(ke["fp32"]), np.mean(ke["fp64"])
-    out["ke_time_avg_rel_diff"] = float(abs(ke32 - ke64) / ke64)
-    out["mean_height_rel_diff"] = float(abs(height["fp32"] - height["fp64"]) / abs(height["fp64"]))
-    out["mean_height_fp64_m"] = height["fp64"]
+    out = {"mean_height_fp64_m": height["fp64"], "ke_time_avg_fp64_J": float(np.mean(ke["fp64"]))}
+    r = res["fp64"]
+    for f in forms:
+        if f not in batches:
+            continue
+        a = res[f]
+        one = {}
+        for k in ("position", "orientation", "velocity", "rotation"):
+            den = np.maximum(np.abs(r[k]).max(axis=1), 1.0)
+            e = np.abs(a[k] - r[k]).max(axis=1) / den
+            one[k] = {"max": float(e.max()), "p99": float(np.quantile(e, 0.99)),
+                      "frac_le_1e-4": float((e <= 1e-4).mean())}
+        out[f] = {"one_step_rel_error": one,
+                  "ke_time_avg_rel_diff": float(abs(np.mean(ke[f]) - np.mean(ke["fp64"])) / np.mean(ke["fp64"])),
+                  "mean_height_rel_diff": float(abs(height[f] - height["fp64"]) / abs(height["fp64"]))}
     return out
 
 
@@ -202,11 +209,20 @@ def run_ours(args):
             dist.barrier()
         torch.cuda.synchronize()
 
-    from cubez_gb300 import autotune
+    from cubez_gb300 import autotune, learned
+    t0 = time.perf_counter()
+    blob, train_info = learned.train_warm_start(num_worlds=args.train_worlds, device=local)
+    train_info["seconds"] = time.perf_counter() - t0
+
+    forms = [("fp32_mlp", FORM_FP32), ("fp32", FORM_FP32), ("fp64", FORM_FP64)]
+    if args.fp32_only:
+        forms = forms[:2]
     batches = {}
     tuning = {}
-    for name, form in (("fp32", FORM_FP32), ("fp64", FORM_FP64)):
+    for name, form in forms:
         b = WorldBatch.from_scene(scene, form=form, device=local)
+        if name == "fp32_mlp":
+            learned.set_warm_start(b, blob)
         if args.autotune:
             # tune on a settled state (half-way through the rollout), untimed
             b.step(frames // 2, DT)
@@ -219,9 +235,12 @@ def run_ours(args):
         batches[name] = b
 
     results = {}
-    for name in ("fp32", "fp64") if not args.fp32_only else ("fp32",):
+    for name, _ in forms:
         b = batches[name]
-        for _ in range(args.warmup):
+        # the float64 comparison form takes ~30 s per rollout: one warm-up and
+        # one timed rollout unless asked otherwise
+        warmup, steps = (args.fp64_warmup, args.fp64_steps) if name == "fp64" else (args.warmup, args.steps)
+        for _ in range(warmup):
             b.restore()
             b.step_timed(frames, DT)
         b.counters(reset=True)
@@ -229,7 +248,7 @@ def run_ours(args):
         launches0 = _lib.kernel_launches()
         clocks = Clocks(local)
         with clocks:
-            for _ in range(args.steps):
+            for _ in range(steps):
                 b.restore()
                 _flush_l2()
                 barrier()
@@ -239,20 +258,20 @@ def run_ours(args):
                 ph_ms += ph
         launches = _lib.kernel_launches() - launches0
         cnt = b.counters()
-        ms = tot_ms / args.steps
+        ms = tot_ms / steps
         if ws > 1:
             import torch.distributed as dist
             tt = torch.tensor([ms], device="cuda")
             dist.all_reduce(tt, op=dist.ReduceOp.MAX)
             ms = float(tt.item())
-        results[name] = {"ms_per_step": ms, "phase_ms": (ph_ms / args.steps).tolist(), "counters": cnt,
-                         "launches": launches, "clocks": clocks.summary(),
+        results[name] = {"ms_per_step": ms, "phase_ms": (ph_ms / steps).tolist(), "counters": cnt,
+                         "launches": launches, "clocks": clocks.summary(), "steps": steps, "warmup": warmup,
                          "value": nb * frames * ws / (ms / 1e3)}
 
-    # e2e through the C ABI with host buffers (precision form)
+    # e2e through the C ABI with host buffers (the headline form)
     e2e = None
     if not args.no_e2e:
-        b = batches["fp32"]
+        b = batches["fp32_mlp"]
         host = {k: np.ascontiguousarray(getattr(scene, k)) for k in scene.FIELDS}
         import ctypes as C
         pinned = {}
@@ -280,9 +299,9 @@ def run_ours(args):
                "d2h_bytes_per_step": real_d2h, "ms_per_step": e2e_s * 1e3}
         del C, out
 
-    acc = accuracy(scene, frames, batches) if not args.no_accuracy else None
+    acc = accuracy(scene, frames, batches) if not args.no_accuracy and "fp64" in batches else None
 
-    r32 = results["fp32"]
+    r32 = results["fp32_mlp"]
     real = 4
     phase_names = ["integrate", "narrowphase", "resolve"]
     ph = r32["phase_ms"]
@@ -297,35 +316,55 @@ def run_ours(args):
         pl = ph[i] / frames
         kernels[n] = {"ms_per_launch": pl, "share": ph[i] / sum(ph), "alg_bytes_per_launch": bl,
                       "gbs": bl / (pl / 1e3) / 1e9}
-    info = batches["fp32"].info()
+    info = batches["fp32_mlp"].info()
     for b in batches.values():
         b.close()
 
     if rank != 0:
         return
     cpu = None if args.no_cpu_baseline else cpu_baseline(args, scene)
+    def block(name):
+        if name not in results:
+            return None
+        r = results[name]
+        return {"value": r["value"], "ms_per_step": r["ms_per_step"], "phase_ms": r["phase_ms"],
+                "steps": r["steps"], "warmup": r["warmup"], "clocks": r["clocks"], "gpu_launches": r["launches"],
+                "counters_per_frame": {k: v / (frames * r["steps"]) for k, v in r["counters"].items()}}
+
+    fp64v = results["fp64"]["value"] if "fp64" in results else None
+    cnt = r32["counters"]
     line = {
         "metric": METRIC, "value": r32["value"], "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": r32["ms_per_step"], "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32 (f64 islands)", "data": "synthetic (seeded scenes)",
+        "vs_baseline": None, "dtype": "f32 (f64 islands) + bf16 MLP", "data": "synthetic (seeded scenes)",
         "config": {"workload": "precision: %d worlds x %d bodies (16 spheres + 16 cubes), %d-frame rollout, "
                                "dt=1/60, iterations 4 x contacts" % (args.worlds, args.bodies, frames),
-                   "form": "fp32 (MLP warm start not yet enabled)", "step": "one %d-frame rollout" % frames,
+                   "form": "fp32 + learned warm start (18-64-64-64-3 BF16 MLP on tensor cores)",
+                   "step": "one %d-frame rollout" % frames,
                    "l2": "explicit 252 MB flush before every timed rollout; working set > L2",
                    "parallelism": "weak: %d worlds per GPU" % args.worlds},
-        "fp64": {"value": results["fp64"]["value"] if "fp64" in results else None,
-                 "ms_per_step": results["fp64"]["ms_per_step"] if "fp64" in results else None,
-                 "phase_ms": results["fp64"]["phase_ms"] if "fp64" in results else None,
-                 "clocks": results["fp64"]["clocks"] if "fp64" in results else None},
-        "fp32_over_fp64": (r32["value"] / results["fp64"]["value"]) if "fp64" in results else None,
+        "fp32_plain": block("fp32"),
+        "fp64": block("fp64"),
+        "mlp_over_fp64": (r32["value"] / fp64v) if fp64v else None,
+        "fp32_plain_over_fp64": (results["fp32"]["value"] / fp64v) if fp64v else None,
+        "mlp_over_fp32_plain": r32["value"] / results["fp32"]["value"],
+        "warm_start": {"training": train_info,
+                       "warm_worlds_per_frame": cnt["warm_worlds"] / (frames * args.steps),
+                       "warm_bodies_per_frame": cnt["warm_bodies"] / (frames * args.steps),
+                       "mean_scale": cnt["warm_scale_sum"] / max(1, cnt["warm_bodies"]),
+                       "fallbacks_per_frame": cnt["warm_fallbacks"] / (frames * args.steps),
+                       "vel_iterations_vs_plain": cnt["vel_iterations"] / max(1, results["fp32"]["counters"]["vel_iterations"])},
         "accuracy": acc,
         "e2e": e2e,
         "gpu_launches": r32["launches"],
         "clocks": r32["clocks"],
         "roofline": {"kernel": phase_names[dom], "bound": "hbm", "achieved": achieved, "peak": peak,
-                     "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind, "traffic": None},
+                     "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind, "traffic": None,
+                     "note": "the resolver is sequential per world and latency / float64-pipe bound; its HBM "
+                             "fraction is reported as asked, iterations per second below"},
+        "resolver_iterations_per_s": (cnt["pos_iterations"] + cnt["vel_iterations"]) / (args.steps * ph[2] / 1e3),
         "kernels": kernels,
-        "counters_per_frame": {k: v / (frames * args.steps) for k, v in r32["counters"].items()},
+        "counters_per_frame": {k: v / (frames * args.steps) for k, v in cnt.items()},
         "batch": info,
         "tuning": tuning,
         "cpu_baseline": cpu,
@@ -393,6 +432,9 @@ def main():
     ap.add_argument("--bodies", type=int, default=32)
     ap.add_argument("--frames", type=int, default=600)
     ap.add_argument("--cpu-worlds", type=int, default=2048)
+    ap.add_argument("--train-worlds", type=int, default=4096)
+    ap.add_argument("--fp64-steps", type=int, default=1)
+    ap.add_argument("--fp64-warmup", type=int, default=1)
     ap.add_argument("--fp32-only", action="store_true")
     ap.add_argument("--autotune", type=int, default=1)
     ap.add_argument("--tune-frames", type=int, default=30)

@@ -123,10 +123,11 @@ class WorldBatch:
         return tot.value, ph
 
     def counters(self, reset=False):
-        a = np.zeros(6, np.int64)
+        a = np.zeros(8, np.int64)
         check(self.L.cz_counters(self.h, _ptr(a), 1 if reset else 0))
         return {"contacts": int(a[0]), "pos_iterations": int(a[1]), "vel_iterations": int(a[2]),
-                "contacts_resolved": int(a[3]), "warm_fallbacks": int(a[4]), "warm_worlds": int(a[5])}
+                "contacts_resolved": int(a[3]), "warm_fallbacks": int(a[4]), "warm_worlds": int(a[5]),
+                "warm_scale_sum": int(a[6]) * 1e-6, "warm_bodies": int(a[7])}
 
     def info(self):
         a = np.zeros(9, np.int64)

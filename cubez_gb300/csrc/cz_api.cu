@@ -111,6 +111,10 @@ struct cz_batch {
   float* hv_labels = nullptr;
   unsigned long long* hv_count = nullptr;
   long long hv_cap = 0;
+  void* ws_rows = nullptr;  // per-body warm-start / harvest scratch (allocated on first use)
+  int* ws_int = nullptr;
+  uint8_t* ws_u8 = nullptr;
+  uint8_t* ws_world = nullptr;
   size_t np_smem = 0, rs_smem = 0;
 
   // graph cache: (nsteps, dt) -> executable graph
@@ -164,6 +168,10 @@ struct cz_batch {
     v.hv_labels = hv_labels;
     v.hv_count = hv_count;
     v.hv_cap = hv_cap;
+    v.ws_rows = ws_rows;
+    v.ws_int = ws_int;
+    v.ws_u8 = ws_u8;
+    v.ws_world = ws_world;
     return v;
   }
 };
@@ -227,7 +235,7 @@ void free_batch(cz_batch* b) {
     cudaGraphExecDestroy(kv.second.exec);
     for (cudaEvent_t e : kv.second.ev) cudaEventDestroy(e);
   }
-  void* dev[] = {b->mlp_mem, b->hv_features, b->hv_labels, b->hv_count, b->snap_body, b->snap_u8, b->body, b->awake, b->can_sleep, b->shape, b->d_bstart, b->d_bcount, b->d_ccap, b->d_ccount,
+  void* dev[] = {b->ws_rows, b->ws_int, b->ws_u8, b->ws_world, b->mlp_mem, b->hv_features, b->hv_labels, b->hv_count, b->snap_body, b->snap_u8, b->body, b->awake, b->can_sleep, b->shape, b->d_bstart, b->d_bcount, b->d_ccap, b->d_ccount,
                  b->d_cstart, b->d_wstatus, b->d_piters, b->d_viters, b->contact, b->cbodies, b->work, b->wbodies,
                  b->d_order, b->d_order_rs, b->d_queue, b->d_status, b->d_counters, b->d_h2p, b->d_stage, b->d_stage_u8, b->d_stage_i32,
                  b->d_cstage, b->d_cstage_b, b->d_pow};
@@ -907,6 +915,18 @@ int cz_step_timed(cz_batch* b, int32_t nsteps, double dt, double* total_ms, doub
   return st;
 }
 
+// The per-body scratch of the warm start and the harvest.
+static int ensure_ws(cz_batch* b) {
+  if (b->ws_rows) return CZ_OK;
+  const size_t P = (size_t)b->nb_pad;
+  CZ_CUDA(cudaMalloc(&b->ws_rows, b->ops->real_size * 13 * P));
+  CZ_CUDA(cudaMalloc((void**)&b->ws_int, sizeof(int) * cz::WS_NINT * P));
+  CZ_CUDA(cudaMalloc((void**)&b->ws_u8, 2 * P));
+  CZ_CUDA(cudaMalloc((void**)&b->ws_world, (size_t)b->num_worlds));
+  CZ_CUDA(cudaMemset(b->ws_world, 0, (size_t)b->num_worlds));
+  return CZ_OK;
+}
+
 int cz_set_warm_start(cz_batch* b, const float* blob) {
   if (!b) return fail(CZ_ERR_BAD_ARG, "cz_set_warm_start: null batch");
   CZ_CUDA(cudaSetDevice(b->device));
@@ -914,6 +934,7 @@ int cz_set_warm_start(cz_batch* b, const float* blob) {
     b->mode = 0;
     return configure(b);
   }
+  if (int st = ensure_ws(b)) return st;
   const size_t blob_bytes = sizeof(float) * cz::MLP_BLOB;
   const size_t off = (blob_bytes + 255) & ~(size_t)255;
   if (!b->mlp_mem) CZ_CUDA(cudaMalloc(&b->mlp_mem, off + cz::mlp_packed_bytes()));
@@ -941,6 +962,7 @@ int cz_harvest(cz_batch* b, int32_t nsteps, double dt, int32_t every, float* fea
     b->hv_cap = capacity;
   }
   if (!b->hv_count) CZ_CUDA(cudaMalloc((void**)&b->hv_count, sizeof(unsigned long long)));
+  if (int st0 = ensure_ws(b)) return st0;
   CZ_CUDA(cudaMemsetAsync(b->hv_count, 0, sizeof(unsigned long long), b->stream));
   int st = ensure_pows(b, dt);
   if (st) return st;
@@ -992,7 +1014,7 @@ int cz_counters(cz_batch* b, int64_t* out, int32_t reset) {
   if (reset) CZ_CUDA(cudaMemsetAsync(b->d_counters, 0, sizeof c, b->stream));
   CZ_CUDA(cudaStreamSynchronize(b->stream));
   if (out)
-    for (int i = 0; i < 6; ++i) out[i] = (int64_t)c[i];
+    for (int i = 0; i < 8; ++i) out[i] = (int64_t)c[i];
   return CZ_OK;
 }
 

@@ -51,6 +51,10 @@ static BatchView<R> view_of(const HostView& h) {
   v.hv_labels = h.hv_labels;
   v.hv_count = h.hv_count;
   v.hv_cap = h.hv_cap;
+  v.ws_rows = static_cast<R*>(h.ws_rows);
+  v.ws_int = h.ws_int;
+  v.ws_u8 = h.ws_u8;
+  v.ws_world = h.ws_world;
   return v;
 }
 
@@ -162,7 +166,8 @@ __global__ void k_set_rows(BatchView<R> v, int row, int nrows, const double* __r
 
 static size_t np_smem(int nbs) { return np_smem_bytes<R>(nbs); }
 static size_t rs_smem(int nbs, int cs, int lanes, int mode) {
-  return (size_t)(32 / lanes) * rs_slot_bytes<R, W>(nbs, cs, mode) + (mode == 2 ? kMlpStageBytes : 0);
+  (void)mode;  // the learned paths keep their scratch in global memory and registers
+  return (size_t)(32 / lanes) * rs_slot_bytes<R, W>(nbs, cs);
 }
 
 // the resolver instantiation for G lanes per world, plain or with the

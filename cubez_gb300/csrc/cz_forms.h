@@ -48,6 +48,10 @@ struct HostView {
   float* hv_labels;
   unsigned long long* hv_count;
   long long hv_cap;
+  void* ws_rows;
+  int* ws_int;
+  uint8_t* ws_u8;
+  uint8_t* ws_world;
 };
 
 // Staging layout of host body data on the device (doubles, field blocks of n):

@@ -13,6 +13,18 @@
 
 namespace cz {
 
+// integer rows of the per-body warm-start scratch
+enum WsInt : int {
+  WS_DEG = 0,   // contacts touching the body
+  WS_NBB,       // contacts between the body and other bodies
+  WS_LOAD,      // sum of their positive desired delta velocities, fixed point 2^-16
+  WS_FIRST,     // first and last index of the body's half-space contacts
+  WS_LAST,
+  WS_SCALE,     // warm-start scale (float bits)
+  WS_NINT
+};
+constexpr float kLoadScale = 65536.f;
+
 enum BodyRow : int {
   B_PX, B_PY, B_PZ,                                      // RigidBody.Position
   B_QW, B_QX, B_QY, B_QZ,                                // RigidBody.Orientation
@@ -109,6 +121,12 @@ template <class R> struct BatchView {
   float* hv_labels;      // harvest output [hv_cap][3]
   unsigned long long* hv_count;
   long long hv_cap;
+  // per-body scratch of the warm start and the harvest (modes 1, 2), indexed
+  // like the body rows (row stride nb_pad)
+  R* ws_rows;            // [13]: saved velocity 0-2, rotation 3-5, motion 6; warm-start change 7-12
+  int* ws_int;           // [WS_NINT]
+  uint8_t* ws_u8;        // [2]: awake flags at the start of adjustVelocities, at prepareContacts
+  uint8_t* ws_world;     // [num_worlds]: the world's last velocity solve used all its iterations
 };
 
 }  // namespace cz

@@ -120,6 +120,43 @@ __device__ __forceinline__ void load_a(const __nv_bfloat16* X, int ld, unsigned 
   }
 }
 
+// A fragments of a 16-row tile whose rows live in lanes 0..15 (row[j] = the
+// lane's own BF16 pair j, columns 2j and 2j + 1), moved by warp shuffles:
+// lane (g, t) takes pairs 8s + t and 8s + 4 + t of rows g and g + 8.  Every
+// lane of the warp calls it.
+__device__ __forceinline__ void rows_to_a(const unsigned (&row)[16], unsigned (&a)[2][4]) {
+  const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+#pragma unroll
+    for (int s = 0; s < 2; ++s) {
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const unsigned lo = __shfl_sync(0xffffffffu, row[8 * s + 4 * h + j], g);
+        const unsigned hi = __shfl_sync(0xffffffffu, row[8 * s + 4 * h + j], g + 8);
+        if (t == j) {
+          a[s][2 * h] = lo;
+          a[s][2 * h + 1] = hi;
+        }
+      }
+    }
+  }
+}
+
+// The three outputs of row `lane & 15` from the accumulators of n-tile 0
+// (row g: o[0], o[1] at columns 2t, 2t + 1; row g + 8: o[2], o[3]).  Every
+// lane of the warp calls it.
+__device__ __forceinline__ void out_to_rows(const float (&o)[4], float (&y)[3]) {
+  const int r = threadIdx.x & 15;
+  const int src = 4 * (r & 7);
+  const float c00 = __shfl_sync(0xffffffffu, o[0], src), c01 = __shfl_sync(0xffffffffu, o[1], src);
+  const float c20 = __shfl_sync(0xffffffffu, o[2], src), c21 = __shfl_sync(0xffffffffu, o[3], src);
+  const float d0 = __shfl_sync(0xffffffffu, o[0], src + 1), d2 = __shfl_sync(0xffffffffu, o[2], src + 1);
+  y[0] = r < 8 ? c00 : c20;
+  y[1] = r < 8 ? c01 : c21;
+  y[2] = r < 8 ? d0 : d2;
+}
+
 // Forward pass of a 16-row tile: input A fragments (normalised features as
 // BF16, K padded to 32) -> output accumulators out[4] of n-tile 0 (columns
 // 2t, 2t+1 of rows g and g+8; columns 0..2 are the normalised impulse).

@@ -30,15 +30,24 @@ template <class R, class W> struct RCtx {
   int* cb;        // packed bodies of this world's contacts
   long long cst;  // row stride of cw
   R* bc;          // broadcast scratch [12]
-  float* deg;     // [nbs] contacts touching each body (warm start / harvest)
-  R* save;        // [6][nbs] velocity and rotation before the warm start
-  R* delta;       // [6][nbs] warm-start velocity and rotation change per body
+  // warm start / harvest (modes 1, 2): this world's per-body scratch in
+  // global memory (row stride wst) and its contacts' impulse rows
+  R* save;        // [7]: velocity 0-2, rotation 3-5, motion 6 at the start of adjustVelocities
+  R* delta;       // [6]: warm-start velocity and rotation change
+  int* wi;        // [WS_NINT] integer rows (WsInt)
+  long long wst;
+  R* jw;          // impulse rows J0..J2 (row stride jst)
+  long long jst;
   const R* gmat;  // friction / restitution rows of the contact list (null: 0.9 / 0.1)
   long long gst;
   R dt;
   __device__ __forceinline__ W& P(int c, int i) const { return bw[c * nbs + i]; }
   __device__ __forceinline__ R& Bf(int r, int i) const { return br[r * nbs + i]; }
   __device__ __forceinline__ R& Cf(int f, int k) const { return cw[(long long)f * cst + k]; }
+  __device__ __forceinline__ R& J(int c, int k) const { return jw[(long long)c * jst + k]; }
+  __device__ __forceinline__ int& WI(int r, int i) const { return wi[(long long)r * wst + i]; }
+  __device__ __forceinline__ R& Save(int r, int i) const { return save[(long long)r * wst + i]; }
+  __device__ __forceinline__ R& Delta(int r, int i) const { return delta[(long long)r * wst + i]; }
   __device__ __forceinline__ v3<R> Bv(int r, int i) const { return V<R>(Bf(r, i), Bf(r + 1, i), Bf(r + 2, i)); }
   __device__ __forceinline__ v3<R> Cv(int f, int k) const { return V<R>(Cf(f, k), Cf(f + 1, k), Cf(f + 2, k)); }
   __device__ __forceinline__ void setCv(int f, int k, const v3<R>& a) const {
@@ -358,9 +367,9 @@ __device__ void apply_velocity_change(const RCtx<R, W>& x, const BatchView<R>& v
     ic = friction_impulse(x, k, b0, b1, C);
   }
   if (LEARN && v.mode == 1) {  // harvest: total impulse applied at this contact
-    x.Cf(W_J0, k) += ic.x;
-    x.Cf(W_J0 + 1, k) += ic.y;
-    x.Cf(W_J0 + 2, k) += ic.z;
+    x.J(0, k) += ic.x;
+    x.J(1, k) += ic.y;
+    x.J(2, k) += ic.z;
   }
   const v3<R> imp = mulv(C, ic);
   const R z = (R)0;
@@ -384,58 +393,44 @@ __device__ void apply_velocity_change(const RCtx<R, W>& x, const BatchView<R>& v
 
 // ---------------------------------------------------------------- world slots
 // Shared memory of one world: body rows (W and R), contact working rows,
-// broadcast scratch, packed bodies, awake flags.  With the learned warm start
-// or harvesting (mode != 0) also the three impulse rows, per-body contact
-// degrees, the saved and delta velocities and two copies of the awake flags.
-template <class R, class W> __host__ __device__ inline size_t rs_slot_bytes(int nbs, int cs, int mode) {
-  const int rows = mode ? W_NROWS : W_NROWS_PLAIN;
+// broadcast scratch, packed bodies, awake flags.  The learned paths keep
+// their per-body scratch and the impulse rows in global memory, so they use
+// the same slot (and reach the same occupancy) as the plain resolver.
+template <class R, class W> __host__ __device__ inline size_t rs_slot_bytes(int nbs, int cs) {
   const size_t nb16 = (size_t)((nbs + 15) & ~15);
   size_t b = (size_t)7 * nbs * sizeof(W);
   b += (size_t)20 * nbs * sizeof(R);
-  b += (size_t)rows * cs * sizeof(R);
+  b += (size_t)W_NROWS_PLAIN * cs * sizeof(R);
   b += 16 * sizeof(R);
-  if (mode) b += (size_t)13 * nbs * sizeof(R) + (size_t)nbs * sizeof(float);
   b += (size_t)cs * sizeof(int);
-  b += nb16 * (mode ? 3 : 1);
+  b += nb16;
   return (b + 15) & ~(size_t)15;
 }
-// staging of one 16-contact tile for the MLP (warm start only): BF16 inputs, FP32 outputs
-constexpr size_t kMlpStageBytes = 16 * MLP_K1 * 2 + 16 * 4 * 4;
 
 template <class R, class W> struct Slot {
   RCtx<R, W> x;
   R* cw_s;
   int* cb_s;
-  uint8_t* aw_pos;  // awake flags at the start of adjustVelocities
-  uint8_t* aw_pre;  // awake flags at prepareContacts
+  uint8_t* aw_pos;  // awake flags at the start of adjustVelocities (global)
+  uint8_t* aw_pre;  // awake flags at prepareContacts (global)
 };
 
 template <class R, class W>
-__device__ __forceinline__ Slot<R, W> make_slot(unsigned char* base, int nbs, int cs, int mode, R dt) {
+__device__ __forceinline__ Slot<R, W> make_slot(unsigned char* base, int nbs, int cs, R dt) {
   Slot<R, W> s;
   RCtx<R, W>& x = s.x;
-  const int rows = mode ? W_NROWS : W_NROWS_PLAIN;
-  const int nb16 = (nbs + 15) & ~15;
   x.nbs = nbs;
   x.dt = dt;
   x.bw = reinterpret_cast<W*>(base);
   x.br = reinterpret_cast<R*>(x.bw + 7 * nbs);
   s.cw_s = x.br + 20 * nbs;
-  x.bc = s.cw_s + (size_t)rows * cs;
-  R* after = x.bc + 16;
-  x.save = x.delta = nullptr;
-  x.deg = nullptr;
-  if (mode) {
-    x.save = after;            // [7][nbs]: vel 0-2, rot 3-5, motion 6
-    x.delta = after + 7 * nbs;  // [6][nbs]
-    x.deg = reinterpret_cast<float*>(after + 13 * nbs);
-    s.cb_s = reinterpret_cast<int*>(x.deg + nbs);
-  } else {
-    s.cb_s = reinterpret_cast<int*>(after);
-  }
+  x.bc = s.cw_s + (size_t)W_NROWS_PLAIN * cs;
+  s.cb_s = reinterpret_cast<int*>(x.bc + 16);
   x.aw = reinterpret_cast<uint8_t*>(s.cb_s + cs);
-  s.aw_pos = mode ? x.aw + nb16 : nullptr;
-  s.aw_pre = mode ? x.aw + 2 * nb16 : nullptr;
+  x.save = x.delta = x.jw = nullptr;
+  x.wi = nullptr;
+  x.wst = x.jst = 0;
+  s.aw_pos = s.aw_pre = nullptr;
   return s;
 }
 
@@ -455,103 +450,209 @@ __device__ __forceinline__ void bind_contacts(Slot<R, W>& s, const BatchView<R>&
   x.gst = (long long)(C_REST - C_FRIC) * v.nc_total;
 }
 
-// The 18 features of a contact at the start of adjustVelocities: normal (3),
-// contact velocity in the contact basis (3), penetration, desired delta
-// velocity (restitution applied), the two inverse masses, the diagonal of
-// each body's world inverse inertia in the contact basis (3 + 3), and the
-// number of contacts touching each body (2).
-template <class R, class W> __device__ void contact_features(const RCtx<R, W>& x, int k, float* f) {
-  const int bb = x.cb[k];
-  const int b[2] = {body0_of(bb), body1_of(bb)};
-  const v3<R> n = x.Cv(W_NX, k), cv = x.Cv(W_CVX, k);
-  f[0] = (float)n.x; f[1] = (float)n.y; f[2] = (float)n.z;
-  f[3] = (float)cv.x; f[4] = (float)cv.y; f[5] = (float)cv.z;
-  f[6] = (float)x.Cf(W_PEN, k);
-  f[7] = (float)x.Cf(W_DDV, k);
-  const m3<R> C = x.basis(k);
-#pragma unroll
-  for (int i = 0; i < 2; ++i) {
-    f[8 + i] = b[i] >= 0 ? (float)x.Bf(18, b[i]) : 0.f;
-    f[16 + i] = b[i] >= 0 ? x.deg[b[i]] : 0.f;
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      float d = 0.f;
-      if (b[i] >= 0) {
-        const v3<R> col = V<R>(C.m[3 * c], C.m[3 * c + 1], C.m[3 * c + 2]);
-        d = (float)dot(col, mulv(x.iit(b[i]), col));
-      }
-      f[10 + 3 * i + c] = d;
-    }
-  }
+// the learned paths' global scratch of the world whose bodies start at bstart
+template <class R, class W>
+__device__ __forceinline__ void bind_ws(Slot<R, W>& s, const BatchView<R>& v, long long bstart, long long cst) {
+  RCtx<R, W>& x = s.x;
+  x.wst = v.nb_pad;
+  x.save = v.ws_rows + bstart;
+  x.delta = v.ws_rows + 7 * v.nb_pad + bstart;
+  x.wi = v.ws_int + bstart;
+  x.jw = v.work + (long long)W_J0 * v.nc_total + cst;
+  x.jst = v.nc_total;
+  s.aw_pos = v.ws_u8 + bstart;
+  s.aw_pre = v.ws_u8 + v.nb_pad + bstart;
 }
 
-// The warm start of one world: every contact's predicted impulse applied at
-// once, bodies accumulating in contact order (deterministic), then every
-// contact's velocity and desired delta velocity brought up to date.  Every
-// lane of the warp calls it (it synchronises the warp); `on` selects the
-// groups whose world is being solved.
+// Contact-frame velocity change per unit impulse of the two bodies together:
+// the matrix calculateFrictionImpulse inverts (contact.go:540-575), here in R
+// alone (a network input, not part of the solve).
+template <class R, class W> __device__ m3<R> response_matrix(const RCtx<R, W>& x, int k, int b0, int b1, const m3<R>& C) {
+  R inv_mass = x.Bf(18, b0);
+  m3<R> itt = skew(x.Cv(W_R0X, k));
+  m3<R> dvw = mulm(mulm(itt, x.iit(b0)), itt);
+  if (b1 >= 0) {
+    itt = skew(x.Cv(W_R1X, k));
+    const m3<R> d2 = mulm(mulm(itt, x.iit(b1)), itt);
+#pragma unroll
+    for (int q = 0; q < 9; ++q) dvw.m[q] += d2.m[q];
+    inv_mass += x.Bf(18, b1);
+  }
+  mulm_with(dvw, (R)-1);
+  m3<R> dv = mulm(mulm(transpose(C), dvw), C);
+  dv.m[0] += inv_mass;
+  dv.m[4] += inv_mass;
+  dv.m[8] += inv_mass;
+  return dv;
+}
+
+// The 18 features of a contact at the start of adjustVelocities, all in the
+// contact basis where they are vectors: the number of contacts between body 0
+// and other bodies, a half-space flag, the contact velocity (3), penetration, desired delta
+// velocity, the response matrix (6: nn, tt, ss, nt, ns, ts), the impulse that
+// would resolve the contact alone along its normal (desired delta velocity /
+// response nn), and per body the contacts touching it and their summed
+// positive desired delta velocities (2 + 2).
+template <class R, class W> __device__ void contact_features(const RCtx<R, W>& x, int k, float* f) {
+  const int bb = x.cb[k];
+  const int b0 = body0_of(bb), b1 = body1_of(bb);
+  const v3<R> cv = x.Cv(W_CVX, k);
+  const R ddv = x.Cf(W_DDV, k);
+  f[0] = (float)x.WI(WS_NBB, b0);
+  f[1] = b1 < 0 ? 1.f : 0.f;
+  f[2] = (float)cv.x; f[3] = (float)cv.y; f[4] = (float)cv.z;
+  f[5] = (float)x.Cf(W_PEN, k);
+  f[6] = (float)ddv;
+  const m3<R> K = response_matrix(x, k, b0, b1, x.basis(k));
+  f[7] = (float)K.m[0]; f[8] = (float)K.m[4]; f[9] = (float)K.m[8];
+  f[10] = (float)K.m[3]; f[11] = (float)K.m[6]; f[12] = (float)K.m[7];
+  f[13] = K.m[0] > (R)0 ? (float)(ddv / K.m[0]) : 0.f;
+  f[14] = (float)x.WI(WS_DEG, b0);
+  f[15] = b1 >= 0 ? (float)x.WI(WS_DEG, b1) : 0.f;
+  f[16] = (float)(unsigned)x.WI(WS_LOAD, b0) * (1.f / kLoadScale);
+  f[17] = b1 >= 0 ? (float)(unsigned)x.WI(WS_LOAD, b1) * (1.f / kLoadScale) : 0.f;
+}
+
+template <int G> __device__ __forceinline__ int group_sum(int v) {
+#pragma unroll
+  for (int off = G / 2; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+  return v;
+}
+
+template <int G, class T> __device__ __forceinline__ T group_min(T v) {
+#pragma unroll
+  for (int off = G / 2; off > 0; off >>= 1) {
+    const T o = __shfl_xor_sync(0xffffffffu, v, off);
+    v = o < v ? o : v;
+  }
+  return v;
+}
+
+// The warm start of one world, for its bodies whose contacts are all with
+// the half-space ("grounded" bodies).  A grounded body's contacts depend on
+// that body's velocity alone, so each one is warm-started independently:
+//  1. Predictions of its contacts are projected: normal impulse >= 0,
+//     friction inside the cone |J_t| <= friction * J_n.  Contacts of other
+//     bodies get none.
+//  2. The body's velocity and rotation change of all those impulses,
+//     accumulated in contact order (deterministic); the half-space contacts
+//     of a body are one run of the contact list when the narrowphase made
+//     them, else the whole list is scanned.
+//  3. A line search picks the body's scale s in [0, 1]: none of its contacts
+//     may be pushed past what resolving it would do (normal velocity at most
+//     velocity + max(desired delta, 0) + the velocity epsilon), and no
+//     tangential speed may grow beyond max(current, epsilon).  The resolver
+//     only removes approaching velocity, so it could not undo an overshoot.
+//  4. The body takes s times its change; its contacts update their velocity
+//     and desired delta velocity as adjustVelocities does after an impulse
+//     (contact.go:416-445).
+// Every lane of the warp calls it (it synchronises the warp); `on` selects
+// the groups whose world is solved.  Adds this lane's warm-started bodies and
+// the sum of their scales to *nw and *ssum.
 template <class R, class W, int G>
-__device__ void apply_warm_start(const RCtx<R, W>& x, int n, int C, int gl, bool on) {
+__device__ void apply_warm_start(const RCtx<R, W>& x, int n, int C, int gl, bool on, int* nw, float* ssum) {
+  const R z = (R)0, eps = (R)0.01;
+  for (int k = gl; on && k < C; k += G) {
+    const int bb = x.cb[k];
+    v3<R> J = V<R>(x.J(0, k), x.J(1, k), x.J(2, k));
+    if (body1_of(bb) >= 0 || x.WI(WS_NBB, body0_of(bb)) != 0 || !(J.x > z)) J = V<R>(z, z, z);  // also NaN
+    const R lim = x.friction(k) * J.x;
+    const R planar = sqrt_<R>(J.y * J.y + J.z * J.z);
+    if (planar > lim) {
+      const R f = planar > z ? lim / planar : z;
+      J.y *= f;
+      J.z *= f;
+    }
+    if (!(planar == planar)) J = V<R>(z, z, z);
+    x.J(0, k) = J.x;
+    x.J(1, k) = J.y;
+    x.J(2, k) = J.z;
+  }
+  __syncwarp();
   for (int i = gl; on && i < n; i += G) {
-    const R z = (R)0;
+    const int deg = x.WI(WS_DEG, i);
+    if (x.WI(WS_NBB, i) != 0 || deg == 0) continue;
     v3<R> dvel = V<R>(z, z, z), drot = V<R>(z, z, z);
     const m3<R> I = x.iit(i);
     const R invm = x.Bf(18, i);
-    for (int k = 0; k < C; ++k) {
-      const int bb = x.cb[k];
-      const int b0 = body0_of(bb), b1 = body1_of(bb);
-      if (b0 != i && b1 != i) continue;
-      const v3<R> J = x.Cv(W_J0, k);
+    const int first = x.WI(WS_FIRST, i), last = x.WI(WS_LAST, i);
+    const bool run = last - first + 1 == deg;
+    for (int k = run ? first : 0; k <= (run ? last : C - 1); ++k) {
+      if (!run && body0_of(x.cb[k]) != i) continue;
+      const v3<R> J = V<R>(x.J(0, k), x.J(1, k), x.J(2, k));
+      if (J.x == z) continue;
       const v3<R> imp = mulv(x.basis(k), J);
-      if (b0 == i) {
-        add(drot, mulv(I, cross(x.Cv(W_R0X, k), imp)));
-        add_scaled(dvel, imp, invm);
-      } else {
-        add(drot, mulv(I, cross(imp, x.Cv(W_R1X, k))));
-        add_scaled(dvel, imp, -invm);
-      }
+      add(drot, mulv(I, cross(x.Cv(W_R0X, k), imp)));
+      add_scaled(dvel, imp, invm);
     }
-    // a body that receives nothing keeps its values bit for bit
-    const bool moved = dvel.x != z || dvel.y != z || dvel.z != z || drot.x != z || drot.y != z || drot.z != z;
 #pragma unroll
     for (int r = 0; r < 3; ++r) {
-      x.delta[r * x.nbs + i] = (&dvel.x)[r];
-      x.delta[(3 + r) * x.nbs + i] = (&drot.x)[r];
-      if (moved) {
-        x.Bf(r, i) += (&dvel.x)[r];
-        x.Bf(3 + r, i) += (&drot.x)[r];
-      }
+      x.Delta(r, i) = (&dvel.x)[r];
+      x.Delta(3 + r, i) = (&drot.x)[r];
     }
+    x.WI(WS_SCALE, i) = __float_as_int(1.f);
   }
   __syncwarp();
-  // contacts touching a moved body: velocity and desired delta velocity as
-  // adjustVelocities updates them after an impulse (contact.go:416-445)
+  // contact velocity change at s = 1 (into the impulse rows) and the largest
+  // scale each contact allows; a body's scale is the smallest of its contacts'
   for (int k = gl; on && k < C; k += G) {
     const int bb = x.cb[k];
-    const int kb[2] = {body0_of(bb), body1_of(bb)};
-    bool touched = false;
-#pragma unroll
-    for (int b = 0; b < 2; ++b) {
-      if (kb[b] < 0) continue;
-#pragma unroll
-      for (int r = 0; r < 6; ++r) touched |= x.delta[r * x.nbs + kb[b]] != (R)0;
-    }
-    if (!touched) continue;
+    const int b0 = body0_of(bb);
+    if (body1_of(bb) >= 0 || x.WI(WS_NBB, b0) != 0) continue;
     const m3<R> Ck = x.basis(k);
-    v3<R> cv = x.Cv(W_CVX, k);
-#pragma unroll
-    for (int b = 0; b < 2; ++b) {
-      const int body = kb[b];
-      if (body < 0) continue;
-      const v3<R> r = b == 0 ? x.Cv(W_R0X, k) : x.Cv(W_R1X, k);
-      const v3<R> dr = V<R>(x.delta[3 * x.nbs + body], x.delta[4 * x.nbs + body], x.delta[5 * x.nbs + body]);
-      const v3<R> dl = V<R>(x.delta[body], x.delta[x.nbs + body], x.delta[2 * x.nbs + body]);
-      v3<R> dv = cross(dr, r);
-      add(dv, dl);
-      v3<R> t = mulv_t(Ck, dv);
-      mul_with(t, b == 1 ? (R)-1 : (R)1);
-      add(cv, t);
+    const v3<R> dr = V<R>(x.Delta(3, b0), x.Delta(4, b0), x.Delta(5, b0));
+    const v3<R> dl = V<R>(x.Delta(0, b0), x.Delta(1, b0), x.Delta(2, b0));
+    v3<R> dv = cross(dr, x.Cv(W_R0X, k));
+    add(dv, dl);
+    const v3<R> dcv = mulv_t(Ck, dv);
+    x.J(0, k) = dcv.x;
+    x.J(1, k) = dcv.y;
+    x.J(2, k) = dcv.z;
+    R sk = (R)1;
+    const R ddv = x.Cf(W_DDV, k);
+    if (dcv.x > z) {
+      const R q = ((ddv > z ? ddv : z) + eps) / dcv.x;
+      if (q < sk) sk = q;
     }
+    const R ty = x.Cf(W_CVY, k), tz = x.Cf(W_CVZ, k);
+    const R a = dcv.y * dcv.y + dcv.z * dcv.z;
+    if (a > z) {
+      const R t2 = ty * ty + tz * tz;
+      const R bound2 = t2 > eps * eps ? t2 : eps * eps;
+      const R hb = ty * dcv.y + tz * dcv.z;
+      // largest s with |t + s dt|^2 <= bound^2: root of a s^2 + 2 hb s + (t2 - bound2)
+      const R disc = hb * hb - a * (t2 - bound2);
+      const R q = (-hb + sqrt_<R>(disc > z ? disc : z)) / a;
+      if (q < sk) sk = q;
+    }
+    float sf = (float)sk;
+    if (!(sf >= 0.f)) sf = 0.f;  // NaN or negative: no warm start
+    if (sf < 1.f) atomicMin(&x.WI(WS_SCALE, b0), __float_as_int(sf));  // non-negative floats order as ints
+  }
+  __syncwarp();
+  for (int i = gl; on && i < n; i += G) {
+    if (x.WI(WS_NBB, i) != 0 || x.WI(WS_DEG, i) == 0) continue;
+    bool moved = false;
+#pragma unroll
+    for (int r = 0; r < 6; ++r) moved |= x.Delta(r, i) != z;
+    if (!moved) continue;
+    const R sb = (R)__int_as_float(x.WI(WS_SCALE, i));
+    ++*nw;
+    *ssum += (float)sb;
+    if (sb == z) continue;
+#pragma unroll
+    for (int r = 0; r < 6; ++r) x.Bf(r, i) += sb * x.Delta(r, i);
+  }
+  __syncwarp();
+  for (int k = gl; on && k < C; k += G) {
+    const int bb = x.cb[k];
+    const int b0 = body0_of(bb);
+    if (body1_of(bb) >= 0 || x.WI(WS_NBB, b0) != 0) continue;
+    const R sb = (R)__int_as_float(x.WI(WS_SCALE, b0));
+    const v3<R> dcv = V<R>(x.J(0, k), x.J(1, k), x.J(2, k));
+    if (sb == z || (dcv.x == z && dcv.y == z && dcv.z == z)) continue;
+    v3<R> cv = x.Cv(W_CVX, k);
+    add_scaled(cv, dcv, sb);
     x.setCv(W_CVX, k, cv);
     x.Cf(W_DDV, k) = desired_dv(x, k);
   }
@@ -629,11 +730,9 @@ __global__ void __launch_bounds__(32) k_resolve(BatchView<R> v, int nbs, int cs,
   const int lane = threadIdx.x;
   const int grp = lane / G, gl = lane % G;
   const int mode = LEARN ? v.mode : 0;
-  const size_t slot_bytes = rs_slot_bytes<R, W>(nbs, cs, mode);
-  Slot<R, W> sl = make_slot<R, W>(smem + (size_t)grp * slot_bytes, nbs, cs, mode, dt);
+  const size_t slot_bytes = rs_slot_bytes<R, W>(nbs, cs);
+  Slot<R, W> sl = make_slot<R, W>(smem + (size_t)grp * slot_bytes, nbs, cs, dt);
   RCtx<R, W>& x = sl.x;
-  __nv_bfloat16* stage_in = reinterpret_cast<__nv_bfloat16*>(smem + (size_t)NG * slot_bytes);
-  float* stage_out = reinterpret_cast<float*>(stage_in + 16 * MLP_K1);
   const long long S = v.nb_pad;
   for (;;) {
     unsigned q0 = 0;
@@ -664,6 +763,7 @@ __global__ void __launch_bounds__(32) k_resolve(BatchView<R> v, int nbs, int cs,
     }
     const long long cst = has ? v.contact_start[w] : 0;
     bind_contacts(sl, v, C, cs, cst);
+    if (LEARN && mode) bind_ws(sl, v, bstart, cst);
     if (active) {
       for (int i = gl; i < n; i += G) {
         const long long g = bstart + i;
@@ -750,23 +850,39 @@ __global__ void __launch_bounds__(32) k_resolve(BatchView<R> v, int nbs, int cs,
     // ---------------- learned warm start / harvest set-up
     const bool solve = active && max_it > 0;
     long long hv_base = -1;
-    if (LEARN && mode && solve) {
-      for (int i = gl; i < n; i += G) {
-        int d = 0;
-        for (int k = 0; k < C; ++k) {
-          const int bb = x.cb[k];
-          d += (body0_of(bb) == i) + (body1_of(bb) == i);
-        }
-        x.deg[i] = (float)d;
+    if (LEARN && mode) {
+      // per-body aggregates by integer atomics (order-free, deterministic)
+      for (int i = gl; solve && i < n; i += G) {
+        x.WI(WS_DEG, i) = 0;
+        x.WI(WS_NBB, i) = 0;
+        x.WI(WS_LOAD, i) = 0;
+        x.WI(WS_FIRST, i) = 0x7fffffff;
+        x.WI(WS_LAST, i) = -1;
         sl.aw_pos[i] = x.aw[i];
 #pragma unroll
-        for (int r = 0; r < 6; ++r) x.save[r * nbs + i] = x.Bf(r, i);
-        x.save[6 * nbs + i] = x.Bf(19, i);
+        for (int r = 0; r < 6; ++r) x.Save(r, i) = x.Bf(r, i);
+        x.Save(6, i) = x.Bf(19, i);
       }
-      for (int k = gl; k < C; k += G) {
-        x.Cf(W_J0, k) = (R)0;
-        x.Cf(W_J0 + 1, k) = (R)0;
-        x.Cf(W_J0 + 2, k) = (R)0;
+      __syncwarp();
+      for (int k = gl; solve && k < C; k += G) {
+        const int bb = x.cb[k];
+        const int b0 = body0_of(bb), b1 = body1_of(bb);
+        const float dd = (float)x.Cf(W_DDV, k);
+        const int fx = dd > 0.f ? (int)(fminf(dd, 100.f) * kLoadScale + 0.5f) : 0;
+        atomicAdd(&x.WI(WS_DEG, b0), 1);
+        atomicAdd(&x.WI(WS_LOAD, b0), fx);
+        if (b1 >= 0) {
+          atomicAdd(&x.WI(WS_DEG, b1), 1);
+          atomicAdd(&x.WI(WS_LOAD, b1), fx);
+          atomicAdd(&x.WI(WS_NBB, b0), 1);
+          atomicAdd(&x.WI(WS_NBB, b1), 1);
+        } else {
+          atomicMin(&x.WI(WS_FIRST, b0), k);
+          atomicMax(&x.WI(WS_LAST, b0), k);
+        }
+        x.J(0, k) = (R)0;
+        x.J(1, k) = (R)0;
+        x.J(2, k) = (R)0;
       }
     }
     __syncwarp();
@@ -780,65 +896,71 @@ __global__ void __launch_bounds__(32) k_resolve(BatchView<R> v, int nbs, int cs,
         for (int k = gl; k < C; k += G) contact_features(x, k, v.hv_features + (hv_base + k) * MLP_IN);
       }
     }
+    bool warmed = false;  // this world had a warm-started body
+    // a world whose last solve used all its iterations is solved plainly:
+    // it would likely use them all again and be re-solved
+    const bool warm_ok = LEARN && mode == 2 && solve && !v.ws_world[w];
     if (LEARN && mode == 2) {
       // inference, one 16-contact tile at a time, over the worlds of this warp
       for (int gi = 0; gi < NG; ++gi) {
-        const int Cg = __shfl_sync(FULL, solve ? C : 0, gi * G);
+        const int Cg = __shfl_sync(FULL, warm_ok ? C : 0, gi * G);
         const long long cstg = __shfl_sync(FULL, cst, gi * G);
+        const int bstg = __shfl_sync(FULL, bstart, gi * G);
         if (Cg == 0) continue;
-        Slot<R, W> sg = make_slot<R, W>(smem + (size_t)gi * slot_bytes, nbs, cs, mode, dt);
+        Slot<R, W> sg = make_slot<R, W>(smem + (size_t)gi * slot_bytes, nbs, cs, dt);
         bind_contacts(sg, v, Cg, cs, cstg);
+        bind_ws(sg, v, bstg, cstg);
         for (int t0 = 0; t0 < Cg; t0 += 16) {
-          if (lane < 16) {
-            const int k = t0 + lane;
-            float f[MLP_IN];
-            if (k < Cg) contact_features(sg.x, k, f);
+          // lanes 0..15 compute one contact's normalised features each; the
+          // tile reaches the MMA fragments and back by shuffles alone
+          unsigned row[16];
+          const int k = t0 + lane;
+          const bool mine = lane < 16 && k < Cg;
+          float f[MLP_IN];
+          if (mine) contact_features(sg.x, k, f);
 #pragma unroll
-            for (int c = 0; c < MLP_K1; c += 2) {
-              float lo = 0.f, hi = 0.f;
-              if (k < Cg && c < MLP_IN) lo = (f[c] - v.mlp.mu[c]) * v.mlp.inv_sigma[c];
-              if (k < Cg && c + 1 < MLP_IN) hi = (f[c + 1] - v.mlp.mu[c + 1]) * v.mlp.inv_sigma[c + 1];
-              *reinterpret_cast<unsigned*>(stage_in + lane * MLP_K1 + c) = pack_bf16(lo, hi);
-            }
+          for (int c = 0; c < MLP_K1; c += 2) {
+            float lo = 0.f, hi = 0.f;
+            if (mine && c < MLP_IN) lo = (f[c] - v.mlp.mu[c]) * v.mlp.inv_sigma[c];
+            if (mine && c + 1 < MLP_IN) hi = (f[c + 1] - v.mlp.mu[c + 1]) * v.mlp.inv_sigma[c + 1];
+            row[c / 2] = pack_bf16(lo, hi);
           }
-          __syncwarp();
           unsigned a[2][4];
-          load_a<2>(stage_in, MLP_K1, a);
-          float o[4];
+          rows_to_a(row, a);
+          float o[4], y[3];
           mlp_forward_tile(v.mlp, a, o);
-          const int g = lane >> 2, t = lane & 3;
-          if (t < 2) {
-            stage_out[g * 4 + 2 * t] = o[0];
-            stage_out[(g + 8) * 4 + 2 * t] = o[2];
-            if (t == 0) {
-              stage_out[g * 4 + 1] = o[1];
-              stage_out[(g + 8) * 4 + 1] = o[3];
-            }
-          }
-          __syncwarp();
-          if (lane < 16 && t0 + lane < Cg) {
+          out_to_rows(o, y);
+          if (mine) {
 #pragma unroll
-            for (int c = 0; c < 3; ++c) sg.x.Cf(W_J0 + c, t0 + lane) = (R)(stage_out[lane * 4 + c] * v.mlp.out_scale[c]);
+            for (int c = 0; c < 3; ++c) sg.x.J(c, k) = (R)(y[c] * v.mlp.out_scale[c]);
           }
-          __syncwarp();
         }
       }
-      apply_warm_start<R, W, G>(x, n, C, gl, solve);
+      int nw = 0;
+      float ssum = 0.f;
+      apply_warm_start<R, W, G>(x, n, C, gl, warm_ok, &nw, &ssum);
       __syncwarp();
+      warmed = group_sum<G>(nw) > 0;
+      if (nw) {
+        atomicAdd(&v.counters[6], (unsigned long long)((double)ssum * 1e6 + 0.5));
+        atomicAdd(&v.counters[7], (unsigned long long)nw);
+      }
     }
     // ---------------- adjustVelocities, contact.go:388-445
     used = velocity_loop<R, W, G, LEARN>(x, v, w, C, gl, max_it, solve);
     int vel_used = used;
     if (LEARN && mode == 2) {
-      // the plain resolver stays the judge: a world that used all its
-      // iterations is solved again by the plain path from the saved state
-      const bool fb = solve && used >= max_it;
+      // the plain resolver stays the judge: a warm-started world that used
+      // all its iterations is solved again by the plain path from the saved
+      // state (a world without a warm-started body was solved plainly)
+      const bool fb = solve && warmed && used >= max_it;
+      if (solve && gl == 0) v.ws_world[w] = used >= max_it;
       if (__any_sync(FULL, fb)) {
         if (fb) {
           for (int i = gl; i < n; i += G) {
 #pragma unroll
-            for (int r = 0; r < 6; ++r) x.Bf(r, i) = x.save[r * nbs + i];
-            x.Bf(19, i) = x.save[6 * nbs + i];
+            for (int r = 0; r < 6; ++r) x.Bf(r, i) = x.Save(r, i);
+            x.Bf(19, i) = x.Save(6, i);
             x.aw[i] = sl.aw_pos[i];
           }
         }
@@ -865,14 +987,14 @@ __global__ void __launch_bounds__(32) k_resolve(BatchView<R> v, int nbs, int cs,
         if (fb) vel_used += used2;
         if (fb && gl == 0) atomicAdd(&v.counters[4], 1ull);
       }
-      if (solve && gl == 0) atomicAdd(&v.counters[5], 1ull);
+      if (warm_ok && gl == 0) atomicAdd(&v.counters[5], 1ull);
     }
     if (LEARN && mode == 1 && hv_base >= 0) {
       for (int k = gl; k < C; k += G) {
         float* lab = v.hv_labels + (hv_base + k) * MLP_OUT;
-        lab[0] = (float)x.Cf(W_J0, k);
-        lab[1] = (float)x.Cf(W_J0 + 1, k);
-        lab[2] = (float)x.Cf(W_J0 + 2, k);
+        lab[0] = (float)x.J(0, k);
+        lab[1] = (float)x.J(1, k);
+        lab[2] = (float)x.J(2, k);
       }
     }
     if (has && gl == 0) {

@@ -114,3 +114,33 @@ class Trainer:
         out = np.zeros((len(x), OUT), np.float32)
         check(self.L.cz_mlp_predict(self.h, _ptr(x), len(x), _ptr(out)))
         return out
+
+
+def train_warm_start(seeds=(100, 101), num_worlds=4096, settle=60, frames=540, every=20, epochs=(16, 16),
+                     lr=(2e-3, 5e-4), batch=8192, max_rows=3_000_000, seed=1, device=0):
+    """The training procedure of the warm-start network: harvest the plain
+    precision-form resolver on seeded precision scenes (settle frames first,
+    then every `every` frames over `frames`), keep the contacts of grounded
+    bodies (all their contacts with the half-space: the ones the warm start
+    serves), train on the GPU in two phases of (epochs, learning rate).
+    Returns (blob, info)."""
+    from . import scenes
+    from .batch import FORM_FP32, WorldBatch
+    xs, ys = [], []
+    for s in seeds:
+        b = WorldBatch.from_scene(scenes.precision(num_worlds=num_worlds, seed=s), form=FORM_FP32, device=device)
+        b.step(settle, 1.0 / 60.0)
+        x, y = harvest(b, frames, 1.0 / 60.0, every=every, capacity=max(1, 2 * max_rows // len(seeds)))
+        b.close()
+        xs.append(x)
+        ys.append(y)
+    x, y = np.concatenate(xs), np.concatenate(ys)
+    grounded = (x[:, 0] == 0) & (x[:, 1] == 1)
+    x, y = x[grounded][:max_rows], y[grounded][:max_rows]
+    t = Trainer(seed=seed, device=device)
+    t.set_data(x, y, normalize=True)
+    losses = [t.train(epochs=e, batch=batch, lr=r) for e, r in zip(epochs, lr)]
+    blob = t.params()
+    t.close()
+    return blob, {"rows": int(len(x)), "grounded_fraction": float(grounded.mean()),
+                  "loss_first": float(losses[0][0]), "loss_last": float(losses[-1][-1]), "seeds": list(seeds)}

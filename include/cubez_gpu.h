@@ -161,8 +161,10 @@ int cz_step_timed(cz_batch* batch, int32_t nsteps, double dt, double* total_ms, 
  * [1] adjustPositions iterations, [2] adjustVelocities iterations (with the
  * warm start: both solves of a re-solved world), [3] contacts resolved,
  * [4] warm-started worlds re-solved by the plain path, [5] warm-started
- * worlds.  reset != 0 zeroes them after reading. */
-int cz_counters(cz_batch* batch, int64_t* out /* [6] */, int32_t reset);
+ * worlds, [6] sum over warm-started bodies of the scale their line search
+ * picked, in millionths, [7] warm-started bodies.  reset != 0 zeroes them
+ * after reading. */
+int cz_counters(cz_batch* batch, int64_t* out /* [8] */, int32_t reset);
 
 /* Sizes: [0] bodies, [1] padded bodies, [2] contact slots, [3] bytes per real,
  * [4] SMs, [5] narrowphase CTAs, [6] resolver CTAs, [7] narrowphase shared
@@ -194,13 +196,18 @@ int cz_resolve_contacts_static(int32_t form, int32_t max_iterations, cz_contact*
  * reference; the precision form's third variant).  A parameter blob is
  * CZ_MLP_BLOB floats: W1[64][18] b1[64] W2[64][64] b2[64] W3[64][64] b3[64]
  * W4[3][64] b4[3] (trainable), then the feature mean[18], 1/std[18] and the
- * output scale[3].  The network maps 18 contact features (normal, contact
- * velocity in the contact basis, penetration, desired delta velocity, the
- * two inverse masses, each body's world inverse inertia diagonal in the
- * contact basis, the contacts touching each body) to the contact-frame
- * impulse the plain resolver applies in total; the predictions are applied
- * before adjustVelocities, which then runs to the reference's epsilons; a
- * world that uses all its iterations is re-solved by the plain path. */
+ * output scale[3].  The network maps 18 contact features (in the contact
+ * basis: the contacts between body 0 and other bodies, a half-space flag,
+ * contact velocity, penetration, desired delta velocity, the 6 entries of
+ * the symmetric velocity-per-impulse matrix, the impulse resolving the
+ * contact alone, and per body the contacts touching it and their summed
+ * positive desired delta velocities) to the contact-frame impulse the plain
+ * resolver applies in total.  Bodies whose contacts are all with the
+ * half-space are warm-started: their predicted impulses are projected onto
+ * the friction cone, scaled by a per-body line search so that no contact is
+ * pushed past its resolved velocity, and applied before adjustVelocities,
+ * which then runs to the reference's epsilons; a world that uses all its
+ * iterations is re-solved by the plain path. */
 #define CZ_MLP_IN 18
 #define CZ_MLP_OUT 3
 #define CZ_MLP_NPARAM 9539
