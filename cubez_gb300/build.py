@@ -15,8 +15,8 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libcubez_gb300.so")
 UNITS = ["cz_fp64.cu", "cz_fp32.cu", "cz_api.cu", "cz_static.cu", "cz_mlp.cu"]
-HEADERS = ["cz_math.cuh", "cz_layout.cuh", "cz_kernels.cuh", "cz_resolve.cuh", "cz_form_impl.cuh", "cz_forms.h",
-           "cz_mlp.cuh"]
+HEADERS = ["cz_math.cuh", "cz_layout.cuh", "cz_kernels.cuh", "cz_resolve.cuh", "cz_resolve_big.cuh",
+           "cz_form_impl.cuh", "cz_forms.h", "cz_mlp.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "--fmad=false", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-fno-fast-math"]
 

@@ -21,6 +21,10 @@
 #include "cz_forms.h"
 #include "cz_layout.cuh"
 
+// Worlds of more bodies than this are resolved by k_resolve_big (bodies and
+// contacts in global memory, one warp per world).
+constexpr int kBigWorld = 64;
+
 namespace {
 
 thread_local std::string g_last_error;
@@ -60,6 +64,15 @@ struct cz_batch {
   std::vector<int> counts, bstart, ccap, h2p;
   std::vector<long long> cstart;
   int max_n = 0, nbs = 4, max_cap = 1;
+  // worlds of more than kBigWorld bodies are resolved by k_resolve_big; the
+  // others by k_resolve with a shared-memory slot of rs_nbs bodies
+  int rs_nbs = 4, nsmall = 0;
+  std::vector<int> big_ids;
+  int* d_big = nullptr;
+  void* big_bw = nullptr;
+  void* big_br = nullptr;
+  uint8_t* big_aw = nullptr;
+  int *big_off = nullptr, *big_cnt = nullptr, *big_adj = nullptr;
 
   // device buffers
   void* body = nullptr;
@@ -172,6 +185,14 @@ struct cz_batch {
     v.ws_int = ws_int;
     v.ws_u8 = ws_u8;
     v.ws_world = ws_world;
+    v.big_list = d_big;
+    v.big_count = (int)big_ids.size();
+    v.big_bw = big_bw;
+    v.big_br = big_br;
+    v.big_aw = big_aw;
+    v.big_off = big_off;
+    v.big_cnt = big_cnt;
+    v.big_adj = big_adj;
     return v;
   }
 };
@@ -235,7 +256,7 @@ void free_batch(cz_batch* b) {
     cudaGraphExecDestroy(kv.second.exec);
     for (cudaEvent_t e : kv.second.ev) cudaEventDestroy(e);
   }
-  void* dev[] = {b->ws_rows, b->ws_int, b->ws_u8, b->ws_world, b->mlp_mem, b->hv_features, b->hv_labels, b->hv_count, b->snap_body, b->snap_u8, b->body, b->awake, b->can_sleep, b->shape, b->d_bstart, b->d_bcount, b->d_ccap, b->d_ccount,
+  void* dev[] = {b->d_big, b->big_bw, b->big_br, b->big_aw, b->big_off, b->big_cnt, b->big_adj, b->ws_rows, b->ws_int, b->ws_u8, b->ws_world, b->mlp_mem, b->hv_features, b->hv_labels, b->hv_count, b->snap_body, b->snap_u8, b->body, b->awake, b->can_sleep, b->shape, b->d_bstart, b->d_bcount, b->d_ccap, b->d_ccount,
                  b->d_cstart, b->d_wstatus, b->d_piters, b->d_viters, b->contact, b->cbodies, b->work, b->wbodies,
                  b->d_order, b->d_order_rs, b->d_queue, b->d_status, b->d_counters, b->d_h2p, b->d_stage, b->d_stage_u8, b->d_stage_i32,
                  b->d_cstage, b->d_cstage_b, b->d_pow};
@@ -295,7 +316,9 @@ int ensure_pows(cz_batch* b, double dt) {
   return CZ_OK;
 }
 
-int launches_per_step(const cz_batch* b) { return 3 + (b->num_worlds > 32 / b->rs_lanes ? 1 : 0); }
+int launches_per_step(const cz_batch* b) {
+  return 2 + (b->nsmall > 0 ? 1 + (b->nsmall > 32 / b->rs_lanes ? 1 : 0) : 0) + (b->big_ids.empty() ? 0 : 1);
+}
 
 int launch_integrate(cz_batch* b, double dt) {
   CZ_CUDA(b->ops->integrate(b->view(), dt, std::pow(0.5, dt), b->int_threads, b->stream));
@@ -308,26 +331,37 @@ int launch_narrowphase(cz_batch* b) {
   g_launches++;
   return CZ_OK;
 }
-int launch_resolve(cz_batch* b, double dt, const cz::HostView* override_view = nullptr) {
-  CZ_CUDA(cudaMemsetAsync(b->d_queue + 1, 0, sizeof(unsigned), b->stream));
-  CZ_CUDA(b->ops->resolve(override_view ? *override_view : b->view(), b->nbs, b->rs_cs, b->rs_lanes, b->rs_grid,
-                          b->rs_smem, dt, b->stream));
-  g_launches++;
-  if (b->num_worlds > 32 / b->rs_lanes) {
-    k_reorder<<<1, 1024, 0, b->stream>>>(b->d_piters, b->d_viters, b->num_worlds, b->d_order_rs);
-    CZ_CUDA(cudaGetLastError());
+// The resolver launches of one frame: k_resolve over the worlds that fit its
+// slot (then the re-queue of those worlds by cost), k_resolve_big over the
+// others.
+int launch_resolve_with(cz_batch* b, double dt, const cz::HostView& v, int cs, size_t smem) {
+  if (b->nsmall > 0) {
+    CZ_CUDA(cudaMemsetAsync(b->d_queue + 1, 0, sizeof(unsigned), b->stream));
+    CZ_CUDA(b->ops->resolve(v, b->rs_nbs, cs, b->rs_lanes, b->rs_grid, smem, dt, b->stream));
+    g_launches++;
+    if (b->nsmall > 32 / b->rs_lanes) {
+      k_reorder<<<1, 1024, 0, b->stream>>>(b->d_piters, b->d_viters, b->num_worlds, b->d_order_rs);
+      CZ_CUDA(cudaGetLastError());
+      g_launches++;
+    }
+  }
+  if (!b->big_ids.empty()) {
+    CZ_CUDA(b->ops->resolve_big(v, (int)b->big_ids.size(), dt, b->stream));
     g_launches++;
   }
   return CZ_OK;
+}
+int launch_resolve(cz_batch* b, double dt, const cz::HostView* override_view = nullptr) {
+  return launch_resolve_with(b, dt, override_view ? *override_view : b->view(), b->rs_cs, b->rs_smem);
 }
 
 int configure(cz_batch* b) {
   // resolver shared-memory tile: shrink the contact capacity until it fits
   int cs = std::min<long long>(b->rs_cs, round_up(b->max_cap, 32));
   cs = std::max(cs, 32);
-  while (cs > 32 && b->ops->rs_smem(b->nbs, cs, b->rs_lanes, b->mode) > b->smem_optin) cs -= 32;
+  while (cs > 32 && b->ops->rs_smem(b->rs_nbs, cs, b->rs_lanes, b->mode) > b->smem_optin) cs -= 32;
   b->rs_cs = cs;
-  b->rs_smem = b->ops->rs_smem(b->nbs, cs, b->rs_lanes, b->mode);
+  b->rs_smem = b->ops->rs_smem(b->rs_nbs, cs, b->rs_lanes, b->mode);
   b->np_smem = b->ops->np_smem(b->nbs);
   if (b->np_smem > b->smem_optin || b->rs_smem > b->smem_optin)
     return fail(CZ_ERR_BODY_LIMIT, "world too large for the shared-memory tiles");
@@ -338,7 +372,7 @@ int configure(cz_batch* b) {
   rsb = std::max(rsb, 1);
   if (b->rs_ctas_per_sm > 0) rsb = std::min(rsb, b->rs_ctas_per_sm);
   b->np_grid = (int)std::min<long long>(b->num_worlds, (long long)npb * b->sm_count);
-  const long long groups = (b->num_worlds + 32 / b->rs_lanes - 1) / (32 / b->rs_lanes);
+  const long long groups = (std::max(b->nsmall, 1) + 32 / b->rs_lanes - 1) / (32 / b->rs_lanes);
   b->rs_grid = (int)std::min<long long>(groups, (long long)rsb * b->sm_count);
   b->np_grid = std::max(b->np_grid, 1);
   b->rs_grid = std::max(b->rs_grid, 1);
@@ -430,6 +464,15 @@ int cz_batch_create(const cz_batch_desc* d, cz_batch** out) {
   b->nb_pad = std::max<long long>(np, 4);
   b->nc_total = std::max<long long>(nc, 4);
   b->nbs = (int)std::max<long long>(round_up(b->max_n, 4), 4);
+  int max_small = 0;
+  for (int w = 0; w < b->num_worlds; ++w) {
+    if (b->counts[w] > kBigWorld)
+      b->big_ids.push_back(w);
+    else
+      max_small = std::max(max_small, b->counts[w]);
+  }
+  b->nsmall = b->num_worlds - (int)b->big_ids.size();
+  b->rs_nbs = (int)std::max<long long>(round_up(max_small, 4), 4);
   b->np_threads = b->max_n >= 256 ? 256 : 128;
   b->rs_cs = d->form == CZ_FORM_FP64 ? 96 : 128;
   b->rs_lanes = d->form == CZ_FORM_FP64 ? 4 : 8;
@@ -465,6 +508,12 @@ int cz_batch_create(const cz_batch_desc* d, cz_batch** out) {
        dmalloc((void**)&b->d_cstage_b, sizeof(int) * b->max_cap);
   ok = ok && dmalloc((void**)&b->d_pow, sizeof(double) * 2 * P);
   ok = ok && dmalloc(&b->snap_body, R * cz::B_NROWS * P) && dmalloc((void**)&b->snap_u8, 2 * P);
+  if (!b->big_ids.empty()) {
+    ok = ok && dmalloc((void**)&b->d_big, sizeof(int) * b->big_ids.size()) &&
+         dmalloc(&b->big_bw, sizeof(double) * 7 * P) && dmalloc(&b->big_br, R * 20 * P) &&
+         dmalloc((void**)&b->big_aw, P) && dmalloc((void**)&b->big_off, sizeof(int) * P) &&
+         dmalloc((void**)&b->big_cnt, sizeof(int) * P) && dmalloc((void**)&b->big_adj, sizeof(int) * 2 * C);
+  }
   if (!ok) return bail(fail(CZ_ERR_CUDA, "device allocation failed"));
   ok = cudaMallocHost((void**)&b->h_stage, sizeof(double) * cz::SG_NDOUBLES * std::max<long long>(nb, 1)) ==
            cudaSuccess &&
@@ -495,6 +544,8 @@ int cz_batch_create(const cz_batch_desc* d, cz_batch** out) {
           cudaSuccess ||
       cudaMemcpyAsync(b->d_order, order.data(), sizeof(int) * W, cudaMemcpyHostToDevice, s) != cudaSuccess ||
       cudaMemcpyAsync(b->d_order_rs, order.data(), sizeof(int) * W, cudaMemcpyHostToDevice, s) != cudaSuccess ||
+      (!b->big_ids.empty() && cudaMemcpyAsync(b->d_big, b->big_ids.data(), sizeof(int) * b->big_ids.size(),
+                                              cudaMemcpyHostToDevice, s) != cudaSuccess) ||
       (nb > 0 &&
        cudaMemcpyAsync(b->d_h2p, b->h2p.data(), sizeof(int) * nb, cudaMemcpyHostToDevice, s) != cudaSuccess) ||
       cudaStreamSynchronize(s) != cudaSuccess)
@@ -970,8 +1021,8 @@ int cz_harvest(cz_batch* b, int32_t nsteps, double dt, int32_t every, float* fea
   // the plain resolver, writing features and applied impulses every `every` frames
   const int saved_mode = b->mode;
   int cs = b->rs_cs;
-  while (cs > 32 && b->ops->rs_smem(b->nbs, cs, b->rs_lanes, 1) > b->smem_optin) cs -= 32;
-  const size_t smem1 = b->ops->rs_smem(b->nbs, cs, b->rs_lanes, 1);
+  while (cs > 32 && b->ops->rs_smem(b->rs_nbs, cs, b->rs_lanes, 1) > b->smem_optin) cs -= 32;
+  const size_t smem1 = b->ops->rs_smem(b->rs_nbs, cs, b->rs_lanes, 1);
   CZ_CUDA(b->ops->prepare(b->np_smem, smem1, b->rs_lanes));
   for (int s = 0; s < nsteps && st == CZ_OK; ++s) {
     st = launch_integrate(b, dt);
@@ -981,15 +1032,7 @@ int cz_harvest(cz_batch* b, int32_t nsteps, double dt, int32_t every, float* fea
       cz::HostView v = b->view();
       v.mode = h ? 1 : 0;
       v.hv_cap = b->hv_cap;
-      CZ_CUDA(cudaMemsetAsync(b->d_queue + 1, 0, sizeof(unsigned), b->stream));
-      CZ_CUDA(b->ops->resolve(v, b->nbs, h ? cs : b->rs_cs, b->rs_lanes, b->rs_grid, h ? smem1 : b->rs_smem, dt,
-                              b->stream));
-      g_launches++;
-      if (b->num_worlds > 32 / b->rs_lanes) {
-        k_reorder<<<1, 1024, 0, b->stream>>>(b->d_piters, b->d_viters, b->num_worlds, b->d_order_rs);
-        CZ_CUDA(cudaGetLastError());
-        g_launches++;
-      }
+      st = launch_resolve_with(b, dt, v, h ? cs : b->rs_cs, h ? smem1 : b->rs_smem);
     }
   }
   b->mode = saved_mode;

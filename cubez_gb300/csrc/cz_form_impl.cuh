@@ -55,6 +55,14 @@ static BatchView<R> view_of(const HostView& h) {
   v.ws_int = h.ws_int;
   v.ws_u8 = h.ws_u8;
   v.ws_world = h.ws_world;
+  v.big_list = h.big_list;
+  v.big_count = h.big_count;
+  v.big_bw = h.big_bw;
+  v.big_br = static_cast<R*>(h.big_br);
+  v.big_aw = h.big_aw;
+  v.big_off = h.big_off;
+  v.big_cnt = h.big_cnt;
+  v.big_adj = h.big_adj;
   return v;
 }
 
@@ -238,6 +246,12 @@ static cudaError_t resolve(const HostView& h, int nbs, int cs, int lanes, int gr
   return cudaGetLastError();
 }
 
+static cudaError_t resolve_big(const HostView& h, int nbig, double dt, cudaStream_t s) {
+  if (nbig <= 0) return cudaSuccess;
+  k_resolve_big<R, W><<<nbig, 32, 0, s>>>(view_of(h), (R)dt);
+  return cudaGetLastError();
+}
+
 static cudaError_t upload(const HostView& h, const double* sg, const uint8_t* u8, const int* i32, const int* h2p,
                           int nb, int has_iw, int has_lfa, cudaStream_t s) {
   if (nb <= 0) return cudaSuccess;
@@ -288,6 +302,7 @@ const FormOps CZ_FORM_OBJ = {sizeof(CZ_R),
                              CZ_FORM_NS::prepare,
                              CZ_FORM_NS::integrate,
                              CZ_FORM_NS::narrowphase,
+                             CZ_FORM_NS::resolve_big,
                              CZ_FORM_NS::resolve,
                              CZ_FORM_NS::upload,
                              CZ_FORM_NS::download,

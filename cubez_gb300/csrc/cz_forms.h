@@ -52,6 +52,14 @@ struct HostView {
   int* ws_int;
   uint8_t* ws_u8;
   uint8_t* ws_world;
+  const int* big_list;
+  int big_count;
+  void* big_bw;
+  void* big_br;
+  uint8_t* big_aw;
+  int* big_off;
+  int* big_cnt;
+  int* big_adj;
 };
 
 // Staging layout of host body data on the device (doubles, field blocks of n):
@@ -67,6 +75,7 @@ struct FormOps {
   cudaError_t (*prepare)(size_t np_smem, size_t rs_smem, int lanes);  // function attributes
   cudaError_t (*integrate)(const HostView& v, double dt, double sleep_bias, int threads, cudaStream_t s);
   cudaError_t (*narrowphase)(const HostView& v, int nbs, int threads, int grid, size_t smem, cudaStream_t s);
+  cudaError_t (*resolve_big)(const HostView& v, int nbig, double dt, cudaStream_t s);
   cudaError_t (*resolve)(const HostView& v, int nbs, int cs, int lanes, int grid, size_t smem, double dt,
                          cudaStream_t s);
   cudaError_t (*upload)(const HostView& v, const double* stage, const uint8_t* u8, const int* i32, const int* h2p,

@@ -640,3 +640,4 @@ __global__ void __launch_bounds__(256) k_narrowphase(BatchView<R> v, int nbs) {
 }  // namespace cz
 
 #include "cz_resolve.cuh"
+#include "cz_resolve_big.cuh"

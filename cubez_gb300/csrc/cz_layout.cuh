@@ -127,6 +127,15 @@ template <class R> struct BatchView {
   int* ws_int;           // [WS_NINT]
   uint8_t* ws_u8;        // [2]: awake flags at the start of adjustVelocities, at prepareContacts
   uint8_t* ws_world;     // [num_worlds]: the world's last velocity solve used all its iterations
+  // worlds above the shared-memory slot of k_resolve, resolved by k_resolve_big
+  const int* big_list;   // [big_count] world ids
+  int big_count;
+  void* big_bw;          // [7][nb_pad] positions / orientations in the island type
+  R* big_br;             // [20][nb_pad] velocity, rotation, lfa, iitWorld, inverse mass, motion
+  uint8_t* big_aw;       // [nb_pad] awake flags
+  int* big_off;          // [nb_pad] start of each body's contact list in its world's segment
+  int* big_cnt;          // [nb_pad] end of each body's contact list
+  int* big_adj;          // [2 * nc_total] contact lists, a world's segment at 2 * contact_start
 };
 
 }  // namespace cz

@@ -658,6 +658,65 @@ __device__ void apply_warm_start(const RCtx<R, W>& x, int n, int C, int gl, bool
   }
 }
 
+// adjustPositions' update of contact k after resolving a contact between
+// bodies d0, d1 (d1 < 0: none) whose linear / angular changes are in x.bc
+// (contact.go:254-280); a contact touching neither is left alone.
+template <class R, class W>
+__device__ __forceinline__ void penetration_update(const RCtx<R, W>& x, int k, int d0, int d1) {
+  const int bb = x.cb[k];
+  const int kb[2] = {body0_of(bb), body1_of(bb)};
+  const bool m0 = kb[0] == d0 || (d1 >= 0 && kb[0] == d1);
+  const bool m1 = kb[1] >= 0 && (kb[1] == d0 || kb[1] == d1);
+  if (!m0 && !m1) return;
+  const v3<R> nk = x.Cv(W_NX, k);
+  R pen = x.Cf(W_PEN, k);
+#pragma unroll
+  for (int b = 0; b < 2; ++b) {
+    if (kb[b] < 0) continue;
+    const v3<R> r = b == 0 ? x.Cv(W_R0X, k) : x.Cv(W_R1X, k);
+#pragma unroll
+    for (int d = 0; d < 2; ++d) {
+      if (kb[b] == (d == 0 ? d0 : d1)) {
+        v3<R> dp = cross(V<R>(x.bc[6 + 3 * d], x.bc[7 + 3 * d], x.bc[8 + 3 * d]), r);
+        add(dp, V<R>(x.bc[3 * d], x.bc[3 * d + 1], x.bc[3 * d + 2]));
+        const R sign = b == 0 ? (R)-1 : (R)1;
+        pen += dot(dp, nk) * sign;
+      }
+    }
+  }
+  x.Cf(W_PEN, k) = pen;
+}
+
+// adjustVelocities' update of contact k (contact.go:412-440), as above.
+template <class R, class W>
+__device__ __forceinline__ void velocity_update(const RCtx<R, W>& x, int k, int d0, int d1) {
+  const int bb = x.cb[k];
+  const int kb[2] = {body0_of(bb), body1_of(bb)};
+  const bool m0 = kb[0] == d0 || (d1 >= 0 && kb[0] == d1);
+  const bool m1 = kb[1] >= 0 && (kb[1] == d0 || kb[1] == d1);
+  if (!m0 && !m1) return;
+  const m3<R> Ck = x.basis(k);
+  v3<R> cv = x.Cv(W_CVX, k);
+#pragma unroll
+  for (int b = 0; b < 2; ++b) {
+    if (kb[b] < 0) continue;
+    const v3<R> r = b == 0 ? x.Cv(W_R0X, k) : x.Cv(W_R1X, k);
+#pragma unroll
+    for (int d = 0; d < 2; ++d) {
+      if (kb[b] == (d == 0 ? d0 : d1)) {
+        v3<R> dv = cross(V<R>(x.bc[6 + 3 * d], x.bc[7 + 3 * d], x.bc[8 + 3 * d]), r);
+        add(dv, V<R>(x.bc[3 * d], x.bc[3 * d + 1], x.bc[3 * d + 2]));
+        const R sign = b == 1 ? (R)-1 : (R)1;
+        v3<R> t = mulv_t(Ck, dv);
+        mul_with(t, sign);
+        add(cv, t);
+      }
+    }
+  }
+  x.setCv(W_CVX, k, cv);
+  x.Cf(W_DDV, k) = desired_dv(x, k);
+}
+
 // adjustVelocities, contact.go:388-445, for the groups with run set; returns
 // the iterations used.
 template <class R, class W, int G, bool LEARN>
@@ -685,33 +744,7 @@ __device__ int velocity_loop(const RCtx<R, W>& x, const BatchView<R>& v, int w, 
     if (run) {
       const int rb = x.cb[bidx];
       const int d0 = body0_of(rb), d1 = body1_of(rb);
-      for (int k = gl; k < C; k += G) {
-        const int bb = x.cb[k];
-        const int kb[2] = {body0_of(bb), body1_of(bb)};
-        const bool m0 = kb[0] == d0 || (d1 >= 0 && kb[0] == d1);
-        const bool m1 = kb[1] >= 0 && (kb[1] == d0 || kb[1] == d1);
-        if (!m0 && !m1) continue;
-        const m3<R> Ck = x.basis(k);
-        v3<R> cv = x.Cv(W_CVX, k);
-#pragma unroll
-        for (int b = 0; b < 2; ++b) {
-          if (kb[b] < 0) continue;
-          const v3<R> r = b == 0 ? x.Cv(W_R0X, k) : x.Cv(W_R1X, k);
-#pragma unroll
-          for (int d = 0; d < 2; ++d) {
-            if (kb[b] == (d == 0 ? d0 : d1)) {
-              v3<R> dv = cross(V<R>(x.bc[6 + 3 * d], x.bc[7 + 3 * d], x.bc[8 + 3 * d]), r);
-              add(dv, V<R>(x.bc[3 * d], x.bc[3 * d + 1], x.bc[3 * d + 2]));
-              const R sign = b == 1 ? (R)-1 : (R)1;
-              v3<R> t = mulv_t(Ck, dv);
-              mul_with(t, sign);
-              add(cv, t);
-            }
-          }
-        }
-        x.setCv(W_CVX, k, cv);
-        x.Cf(W_DDV, k) = desired_dv(x, k);
-      }
+      for (int k = gl; k < C; k += G) velocity_update(x, k, d0, d1);
     }
     __syncwarp();
     if (run && ++used >= max_it) run = false;
@@ -740,8 +773,9 @@ __global__ void __launch_bounds__(32) k_resolve(BatchView<R> v, int nbs, int cs,
     q0 = __shfl_sync(FULL, q0, 0);
     if (q0 >= (unsigned)v.num_worlds) break;
     const unsigned qi = q0 + grp;
-    const bool has = qi < (unsigned)v.num_worlds;
+    bool has = qi < (unsigned)v.num_worlds;
     const int w = has ? v.order_rs[qi] : 0;
+    if (has && v.big_count > 0 && v.body_count[w] > nbs) has = false;  // a world of k_resolve_big
     const int n = has ? v.body_count[w] : 0;
     const int bstart = has ? v.body_start[w] : 0;
     int C = has ? v.contact_count[w] : 0;
@@ -818,30 +852,7 @@ __global__ void __launch_bounds__(32) k_resolve(BatchView<R> v, int nbs, int cs,
       if (run) {
         const int rb = x.cb[bidx];
         const int d0 = body0_of(rb), d1 = body1_of(rb);
-        for (int k = gl; k < C; k += G) {
-          const int bb = x.cb[k];
-          const int kb[2] = {body0_of(bb), body1_of(bb)};
-          const bool m0 = kb[0] == d0 || (d1 >= 0 && kb[0] == d1);
-          const bool m1 = kb[1] >= 0 && (kb[1] == d0 || kb[1] == d1);
-          if (!m0 && !m1) continue;
-          const v3<R> nk = x.Cv(W_NX, k);
-          R pen = x.Cf(W_PEN, k);
-#pragma unroll
-          for (int b = 0; b < 2; ++b) {
-            if (kb[b] < 0) continue;
-            const v3<R> r = b == 0 ? x.Cv(W_R0X, k) : x.Cv(W_R1X, k);
-#pragma unroll
-            for (int d = 0; d < 2; ++d) {
-              if (kb[b] == (d == 0 ? d0 : d1)) {
-                v3<R> dp = cross(V<R>(x.bc[6 + 3 * d], x.bc[7 + 3 * d], x.bc[8 + 3 * d]), r);
-                add(dp, V<R>(x.bc[3 * d], x.bc[3 * d + 1], x.bc[3 * d + 2]));
-                const R sign = b == 0 ? (R)-1 : (R)1;
-                pen += dot(dp, nk) * sign;
-              }
-            }
-          }
-          x.Cf(W_PEN, k) = pen;
-        }
+        for (int k = gl; k < C; k += G) penetration_update(x, k, d0, d1);
       }
       __syncwarp();
       if (run && ++used >= max_it) run = false;

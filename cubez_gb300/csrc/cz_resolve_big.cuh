@@ -1,0 +1,224 @@
+// ResolveContacts (contact.go:204-445) for worlds whose bodies do not fit the
+// shared-memory slot of k_resolve (hundreds to thousands of bodies).
+//
+// One warp per world.  Body and contact working rows live in global memory
+// (L2-resident at these sizes); the argmax over the world's contacts is the
+// same lane-strided scan and first-maximum butterfly as k_resolve.  After
+// prepareContacts every body gets the list of its contacts (counting sort by
+// body, in global memory), so the update after each resolved contact visits
+// only the contacts of the two resolved bodies instead of all C: the
+// reference's loop over every contact skips the others, so the visited set
+// and each contact's arithmetic are the same (penetration_update /
+// velocity_update), and the float64 form stays bit-identical.  The order of
+// the visits does not matter: each contact's update reads only its own rows
+// and the resolved contact's broadcast changes.
+#pragma once
+#include "cz_resolve.cuh"
+
+namespace cz {
+
+// Visit every contact of bodies d0 and d1 once (lists adj[off[b] .. end[b])).
+template <class R, class W, class F>
+__device__ __forceinline__ void for_pair_contacts(const RCtx<R, W>& x, const int* __restrict__ adj, const int* off,
+                                                  const int* end, int d0, int d1, int lane, F f) {
+  const int o0 = off[d0], l0 = end[d0] - o0;
+  const int o1 = d1 >= 0 ? off[d1] : 0, l1 = d1 >= 0 ? end[d1] - o1 : 0;
+  for (int e = lane; e < l0 + l1; e += 32) {
+    int k;
+    if (e < l0) {
+      k = adj[o0 + e];
+    } else {
+      k = adj[o1 + e - l0];
+      const int bb = x.cb[k];
+      if (body0_of(bb) == d0 || body1_of(bb) == d0) continue;  // visited in d0's list
+    }
+    f(k);
+  }
+}
+
+template <class R, class W>
+__global__ void __launch_bounds__(32) k_resolve_big(BatchView<R> v, R dt) {
+  __shared__ R bc[16];
+  const int lane = threadIdx.x;
+  const int w = v.big_list[blockIdx.x];
+  const int n = v.body_count[w];
+  const int bstart = v.body_start[w];
+  const long long cst = v.contact_start[w];
+  const long long S = v.nb_pad;
+  int C = v.contact_count[w];
+  const int cap = v.contact_cap[w];
+  if (C > cap) C = cap;  // the world is already flagged ST_CAPACITY
+  RCtx<R, W> x;
+  x.nbs = (int)S;  // row stride of the global body rows
+  x.dt = dt;
+  x.bw = reinterpret_cast<W*>(v.big_bw) + bstart;
+  x.br = v.big_br + bstart;
+  x.aw = v.big_aw + bstart;
+  x.bc = bc;
+  x.cw = v.work + cst;
+  x.cb = v.work_bodies + cst;
+  x.cst = v.nc_total;
+  x.gmat = v.uniform_material ? nullptr : v.contact + (long long)C_FRIC * v.nc_total + cst;
+  x.gst = (long long)(C_REST - C_FRIC) * v.nc_total;
+  x.save = x.delta = x.jw = nullptr;
+  x.wi = nullptr;
+  x.wst = x.jst = 0;
+  const bool active = C > 0 && dt > (R)0;  // ResolveContacts guards, contact.go:210-212
+  if (!active) {
+    if (lane == 0) {
+      v.pos_iters[w] = 0;
+      v.vel_iters[w] = 0;
+      atomicAdd(&v.counters[3], (unsigned long long)C);
+    }
+    return;  // the whole block (one warp) leaves together
+  }
+  for (int i = lane; i < n; i += 32) {
+    const long long g = bstart + i;
+    x.P(0, i) = (W)v.body[B_PX * S + g];
+    x.P(1, i) = (W)v.body[B_PY * S + g];
+    x.P(2, i) = (W)v.body[B_PZ * S + g];
+    x.P(3, i) = (W)v.body[B_QW * S + g];
+    x.P(4, i) = (W)v.body[B_QX * S + g];
+    x.P(5, i) = (W)v.body[B_QY * S + g];
+    x.P(6, i) = (W)v.body[B_QZ * S + g];
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+      x.Bf(r, i) = v.body[(B_VX + r) * S + g];
+      x.Bf(3 + r, i) = v.body[(B_RX + r) * S + g];
+      x.Bf(6 + r, i) = v.body[(B_LX + r) * S + g];
+    }
+#pragma unroll
+    for (int r = 0; r < 9; ++r) x.Bf(9 + r, i) = v.body[(B_IW0 + r) * S + g];
+    x.Bf(18, i) = v.body[B_INVM * S + g];
+    x.Bf(19, i) = v.body[B_MOTION * S + g];
+    x.aw[i] = v.awake[g];
+  }
+  __syncwarp();
+  for (int k = lane; k < C; k += 32) prepare_contact(x, v, cst + k, k);
+  __syncwarp();
+  // contact lists per body: count, exclusive scan, fill
+  int* off = v.big_off + bstart;
+  int* end = v.big_cnt + bstart;  // counts, then the fill cursor, then the list ends
+  int* adj = v.big_adj + 2 * cst;
+  for (int i = lane; i < n; i += 32) end[i] = 0;
+  __syncwarp();
+  for (int k = lane; k < C; k += 32) {
+    const int bb = x.cb[k];
+    atomicAdd(&end[body0_of(bb)], 1);
+    if (body1_of(bb) >= 0) atomicAdd(&end[body1_of(bb)], 1);
+  }
+  __syncwarp();
+  int carry = 0;
+  for (int base = 0; base < n; base += 32) {
+    const int i = base + lane;
+    const int c = i < n ? end[i] : 0;
+    int s = c;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const int y = __shfl_up_sync(FULL, s, d);
+      if (lane >= d) s += y;
+    }
+    if (i < n) {
+      off[i] = carry + s - c;
+      end[i] = carry + s - c;
+    }
+    carry += __shfl_sync(FULL, s, 31);
+  }
+  __syncwarp();
+  for (int k = lane; k < C; k += 32) {
+    const int bb = x.cb[k];
+    adj[atomicAdd(&end[body0_of(bb)], 1)] = k;
+    if (body1_of(bb) >= 0) adj[atomicAdd(&end[body1_of(bb)], 1)] = k;
+  }
+  __syncwarp();
+  const int max_it = v.max_iterations >= 0 ? v.max_iterations : C * v.iter_mult;
+  // ---------------- adjustPositions, contact.go:231-283
+  int pos_used = 0;
+  while (pos_used < max_it) {
+    auto best = key_of((R)0, (R)0);
+    int bidx = 0x7fffffff;
+    for (int k = lane; k < C; k += 32) {
+      const auto key = key_of(x.Cf(W_PEN, k), (R)0.01);
+      if (key > best) {
+        best = key;
+        bidx = k;
+      }
+    }
+    group_first_max<32>(best, bidx);
+    if (best == 0) break;
+    if (lane == 0) {
+      match_awake(x, x.cb[bidx]);
+      apply_position_change(x, v, bstart, bidx, x.Cf(W_PEN, bidx));
+    }
+    __syncwarp();
+    const int rb = x.cb[bidx];
+    const int d0 = body0_of(rb), d1 = body1_of(rb);
+    for_pair_contacts(x, adj, off, end, d0, d1, lane, [&](int k) { penetration_update(x, k, d0, d1); });
+    __syncwarp();
+    ++pos_used;
+  }
+  // ---------------- adjustVelocities, contact.go:388-445
+  int vel_used = 0;
+  while (vel_used < max_it) {
+    auto best = key_of((R)0, (R)0);
+    int bidx = 0x7fffffff;
+    for (int k = lane; k < C; k += 32) {
+      const auto key = key_of(x.Cf(W_DDV, k), (R)0.01);
+      if (key > best) {
+        best = key;
+        bidx = k;
+      }
+    }
+    group_first_max<32>(best, bidx);
+    if (best == 0) break;
+    if (lane == 0) {
+      match_awake(x, x.cb[bidx]);
+      apply_velocity_change<R, W, false>(x, v, w, bidx);
+    }
+    __syncwarp();
+    const int rb = x.cb[bidx];
+    const int d0 = body0_of(rb), d1 = body1_of(rb);
+    for_pair_contacts(x, adj, off, end, d0, d1, lane, [&](int k) { velocity_update(x, k, d0, d1); });
+    __syncwarp();
+    ++vel_used;
+  }
+  if (lane == 0) {
+    v.pos_iters[w] = pos_used;
+    v.vel_iters[w] = vel_used;
+    atomicAdd(&v.counters[1], (unsigned long long)pos_used);
+    atomicAdd(&v.counters[2], (unsigned long long)vel_used);
+    atomicAdd(&v.counters[3], (unsigned long long)C);
+  }
+  if (v.contact_writeback) {
+    const long long CS = v.nc_total;
+    for (int k = lane; k < C; k += 32) {
+      R* o = v.contact + cst + k;
+      o[C_NX * CS] = x.Cf(W_NX, k);
+      o[C_NY * CS] = x.Cf(W_NY, k);
+      o[C_NZ * CS] = x.Cf(W_NZ, k);
+      o[C_PEN * CS] = x.Cf(W_PEN, k);
+      v.contact_bodies[cst + k] = x.cb[k];
+    }
+  }
+  for (int i = lane; i < n; i += 32) {
+    const long long g = bstart + i;
+    v.body[B_PX * S + g] = (R)x.P(0, i);
+    v.body[B_PY * S + g] = (R)x.P(1, i);
+    v.body[B_PZ * S + g] = (R)x.P(2, i);
+    v.body[B_QW * S + g] = (R)x.P(3, i);
+    v.body[B_QX * S + g] = (R)x.P(4, i);
+    v.body[B_QY * S + g] = (R)x.P(5, i);
+    v.body[B_QZ * S + g] = (R)x.P(6, i);
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+      v.body[(B_VX + r) * S + g] = x.Bf(r, i);
+      v.body[(B_RX + r) * S + g] = x.Bf(3 + r, i);
+    }
+#pragma unroll
+    for (int r = 0; r < 9; ++r) v.body[(B_IW0 + r) * S + g] = x.Bf(9 + r, i);
+    v.body[B_MOTION * S + g] = x.Bf(19, i);
+    v.awake[g] = x.aw[i];
+  }
+}
+
+}  // namespace cz
