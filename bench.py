@@ -25,6 +25,13 @@ per frame).  The metric is body-steps/s = bodies x frames / time.
   cpu_baseline  the oracle (C++ restatement of the reference's float64 Go path)
               on the host's cores, one thread per world, on a bounded sample
 
+--workload piles measures the large-world configuration instead: 256 worlds x
+1024 cubes (16 x 16 x 4 lattice, dropped 0.5 m), 300 frames, float32 and
+float64 forms; metric pair-tests/s (ordered narrowphase pair and half-space
+tests per second over the narrowphase time) with body-steps/s beside it.  The
+learned warm start serves worlds within the resolver's shared-memory slot
+only, so the large worlds run the plain precision form.
+
 --impl reference times the reference's CPU path (the oracle port; the Go
 reference cannot be built here) on all host cores with the same metric.
 """
@@ -422,6 +429,73 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+def run_piles(args):
+    """The large-world configuration: bounded timing (one rollout per form
+    after an untimed warm-up of `--warmup` rollouts, default 0 here: one
+    float64 rollout takes minutes), a CPU sample of one world."""
+    import torch
+    ws, rank, local = _dist()
+    torch.cuda.set_device(local)
+    from cubez_gb300 import _lib, scenes
+    from cubez_gb300.batch import FORM_FP32, FORM_FP64, WorldBatch
+    nw = args.worlds if args.worlds != 16384 else 256
+    frames = args.frames if args.frames != 600 else 300
+    scene = scenes.piles(num_worlds=nw, seed=5 + 1000 * rank)
+    n = int(scene.counts[0])
+    units = nw * (n * (n - 1) + n)  # ordered pair tests + half-space tests per frame
+    out = {}
+    settled = None
+    for name, form in (("fp32", FORM_FP32), ("fp64", FORM_FP64)):
+        b = WorldBatch.from_scene(scene, form=form, device=local)
+        b.prepare_rollout(frames, DT)
+        b.snapshot()
+        for _ in range(args.warmup if args.warmup_given else 0):
+            b.restore()
+            b.step_timed(frames, DT)
+        b.restore()
+        b.counters(reset=True)
+        launches0 = _lib.kernel_launches()
+        clocks = Clocks(local)
+        with clocks:
+            torch.cuda.synchronize()
+            tot, ph = b.step_timed(frames, DT)
+        cnt = b.counters()
+        out[name] = {"ms_per_step": tot, "phase_ms": [float(p) for p in ph], "clocks": clocks.summary(),
+                     "gpu_launches": _lib.kernel_launches() - launches0,
+                     "body_steps_per_s": scene.num_bodies * frames / (tot / 1e3),
+                     "pair_tests_per_s": units * frames / (ph[1] / 1e3),
+                     "counters_per_world_frame": {k: v / (frames * nw) for k, v in cnt.items()}}
+        if name == "fp64":
+            settled = b.download(("position", "orientation", "velocity", "rotation"))
+        b.close()
+    cpu = None
+    if not args.no_cpu_baseline and rank == 0:
+        # one world, 10 frames from the float64 state after the rollout (piles at rest)
+        from oracle.oracle import OracleBatch
+        one = scene.subset([0])
+        for k, v in settled.items():
+            setattr(one, k, v[:n])
+        ob = OracleBatch(one)
+        t0 = time.perf_counter()
+        ob.step(10, DT, 4, 1)
+        el = time.perf_counter() - t0
+        cpu = {"value": n * 10 / el, "unit": UNIT, "cores": 1, "kind": "port",
+               "sample": "1 world x 10 frames from the settled float64 state (float64 oracle, %.1f s)" % el}
+    if rank != 0:
+        return
+    r = out["fp32"]
+    line = {"metric": "pair-tests/s (large worlds, secondary)", "value": r["pair_tests_per_s"], "unit": "pair-tests/s",
+            "n_gpus": ws, "steps": 1, "warmup": args.warmup if args.warmup_given else 0,
+            "ms_per_step": r["ms_per_step"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 (f64 islands)", "data": "synthetic (seeded scenes)",
+            "config": {"workload": "piles: %d worlds x %d cubes (16x16x4 lattice, dropped 0.5 m), %d frames, dt=1/60"
+                                   % (nw, n, frames), "step": "one %d-frame rollout" % frames},
+            "body_steps_per_s": r["body_steps_per_s"], "fp32": r, "fp64": out["fp64"],
+            "fp32_over_fp64": r["body_steps_per_s"] / out["fp64"]["body_steps_per_s"],
+            "gpu_launches": r["gpu_launches"], "clocks": r["clocks"], "cpu_baseline": cpu}
+    print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -433,6 +507,7 @@ def main():
     ap.add_argument("--frames", type=int, default=600)
     ap.add_argument("--cpu-worlds", type=int, default=2048)
     ap.add_argument("--train-worlds", type=int, default=4096)
+    ap.add_argument("--workload", default="precision", choices=["precision", "piles"])
     ap.add_argument("--fp64-steps", type=int, default=1)
     ap.add_argument("--fp64-warmup", type=int, default=1)
     ap.add_argument("--fp32-only", action="store_true")
@@ -442,7 +517,11 @@ def main():
     ap.add_argument("--no-accuracy", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
-    if args.impl == "reference":
+    import sys as _sys
+    args.warmup_given = any(a.startswith("--warmup") for a in _sys.argv[1:])
+    if args.workload == "piles" and args.impl != "reference":
+        run_piles(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)

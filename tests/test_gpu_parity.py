@@ -152,3 +152,20 @@ def test_resolver_lanes_per_world_bit_exact(form, lanes, cuda_lib):
     assert np.array_equal(gs["pos_iterations"], rs["pos_iterations"])
     assert np.array_equal(gs["vel_iterations"], rs["vel_iterations"])
     assert rs["contacts"].max() > 32  # some worlds exceed the shared-memory tile
+
+
+@pytest.mark.parametrize("form", [0, 1])
+def test_sleeping_bodies_bit_exact(form, cuda_lib):
+    """CanSleep on (rigidbody.go:248-258): motion average, SetAwake(false)
+    zeroing the velocities, matchAwakeState waking a partner and the asleep
+    body's CalculateDerivedData inside applyPositionChange (contact.go:185-202,
+    380-382).  The configurations disable sleeping; this exercises the path."""
+    scene = scenes.mixed(num_worlds=24, seed=27, min_bodies=8, max_bodies=40)
+    scene.can_sleep[:] = 1
+    gpu, ref = _pair(scene, form, cuda_lib)
+    for chunk in range(8):
+        gpu.step(60, DT)
+        ref.step(60, DT)
+        g, r = gpu.download(), ref.bodies()
+        assert_bodies_equal(g, r, STATE + ("motion", "is_awake"))
+    assert (g["is_awake"] == 0).sum() > 100  # bodies went to sleep (326 of 585 in the oracle)
