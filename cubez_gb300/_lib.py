@@ -83,6 +83,7 @@ SIGNATURES = {
     "cz_step_timed": (C.c_int, [C.c_void_p, C.c_int32, C.c_double, C.POINTER(C.c_double), C.c_void_p]),
     "cz_batch_info": (C.c_int, [C.c_void_p, C.c_void_p]),
     "cz_counters": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32]),
+    "cz_collide": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_int32]),
     "cz_status_string": (C.c_char_p, [C.c_int]),
     "cz_last_error": (C.c_char_p, []),
     "cz_kernel_launches": (C.c_int64, []),

@@ -103,6 +103,13 @@ class WorldBatch:
     def narrowphase(self):
         check(self.L.cz_narrowphase(self.h))
 
+    def collide(self, world, units, plane=None):
+        """The narrowphase for a list of (i, j) tests of one world, j = -1 for
+        the half-space (cz_collide); the world's contact list is replaced."""
+        u = np.ascontiguousarray(np.asarray(units, dtype=np.int32).reshape(-1, 2))
+        p = None if plane is None else np.ascontiguousarray(plane, dtype=np.float64)
+        check(self.L.cz_collide(self.h, int(world), None if p is None else _ptr(p), _ptr(u), len(u)))
+
     def resolve(self, dt=1.0 / 60.0):
         check(self.L.cz_resolve(self.h, float(dt)))
 

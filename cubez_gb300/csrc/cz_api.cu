@@ -69,6 +69,8 @@ struct cz_batch {
   int rs_nbs = 4, nsmall = 0;
   std::vector<int> big_ids;
   int* d_big = nullptr;
+  int* d_units = nullptr;  // cz_collide's unit list
+  long long units_cap = 0;
   void* big_bw = nullptr;
   void* big_br = nullptr;
   uint8_t* big_aw = nullptr;
@@ -256,7 +258,7 @@ void free_batch(cz_batch* b) {
     cudaGraphExecDestroy(kv.second.exec);
     for (cudaEvent_t e : kv.second.ev) cudaEventDestroy(e);
   }
-  void* dev[] = {b->d_big, b->big_bw, b->big_br, b->big_aw, b->big_off, b->big_cnt, b->big_adj, b->ws_rows, b->ws_int, b->ws_u8, b->ws_world, b->mlp_mem, b->hv_features, b->hv_labels, b->hv_count, b->snap_body, b->snap_u8, b->body, b->awake, b->can_sleep, b->shape, b->d_bstart, b->d_bcount, b->d_ccap, b->d_ccount,
+  void* dev[] = {b->d_units, b->d_big, b->big_bw, b->big_br, b->big_aw, b->big_off, b->big_cnt, b->big_adj, b->ws_rows, b->ws_int, b->ws_u8, b->ws_world, b->mlp_mem, b->hv_features, b->hv_labels, b->hv_count, b->snap_body, b->snap_u8, b->body, b->awake, b->can_sleep, b->shape, b->d_bstart, b->d_bcount, b->d_ccap, b->d_ccount,
                  b->d_cstart, b->d_wstatus, b->d_piters, b->d_viters, b->contact, b->cbodies, b->work, b->wbodies,
                  b->d_order, b->d_order_rs, b->d_queue, b->d_status, b->d_counters, b->d_h2p, b->d_stage, b->d_stage_u8, b->d_stage_i32,
                  b->d_cstage, b->d_cstage_b, b->d_pow};
@@ -976,6 +978,35 @@ static int ensure_ws(cz_batch* b) {
   CZ_CUDA(cudaMalloc((void**)&b->ws_world, (size_t)b->num_worlds));
   CZ_CUDA(cudaMemset(b->ws_world, 0, (size_t)b->num_worlds));
   return CZ_OK;
+}
+
+int cz_collide(cz_batch* b, int32_t world, const double* plane, const int32_t* units, int32_t nunits) {
+  if (!b || world < 0 || world >= b->num_worlds || nunits < 0 || (nunits > 0 && !units))
+    return fail(CZ_ERR_BAD_ARG, "cz_collide: bad argument");
+  const int n = b->counts[world];
+  for (int u = 0; u < nunits; ++u) {
+    const int i = units[2 * u], j = units[2 * u + 1];
+    if (i < 0 || i >= n || j < -1 || j >= n || j == i)
+      return fail(CZ_ERR_BAD_ARG, "cz_collide: unit " + std::to_string(u) + " is not (body, other body or -1)");
+  }
+  CZ_CUDA(cudaSetDevice(b->device));
+  if (nunits > b->units_cap) {
+    cudaFree(b->d_units);
+    b->d_units = nullptr;
+    b->units_cap = 0;
+    CZ_CUDA(cudaMalloc((void**)&b->d_units, sizeof(int) * 2 * (size_t)nunits));
+    b->units_cap = nunits;
+  }
+  if (nunits > 0)
+    CZ_CUDA(cudaMemcpyAsync(b->d_units, units, sizeof(int) * 2 * (size_t)nunits, cudaMemcpyHostToDevice, b->stream));
+  int st = reset_status(b);
+  if (st) return st;
+  cz::HostView v = b->view();
+  if (plane)
+    for (int k = 0; k < 4; ++k) v.plane[k] = plane[k];
+  CZ_CUDA(b->ops->collide(v, world, b->d_units, nunits, b->nbs, b->np_smem, b->stream));
+  g_launches++;
+  return finish(b);
 }
 
 int cz_set_warm_start(cz_batch* b, const float* blob) {

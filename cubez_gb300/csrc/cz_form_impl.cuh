@@ -246,6 +246,19 @@ static cudaError_t resolve(const HostView& h, int nbs, int cs, int lanes, int gr
   return cudaGetLastError();
 }
 
+static cudaError_t collide(const HostView& h, int world, const void* units, int nunits, int nbs, size_t smem,
+                           cudaStream_t s) {
+  const void* f = (const void*)k_collide<R>;
+  cudaFuncAttributes a;
+  cudaError_t e = cudaFuncGetAttributes(&a, f);
+  if (e != cudaSuccess) return e;
+  if ((size_t)a.maxDynamicSharedSizeBytes < smem &&
+      (e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) != cudaSuccess)
+    return e;
+  k_collide<R><<<1, 256, smem, s>>>(view_of(h), world, static_cast<const int2*>(units), nunits, nbs);
+  return cudaGetLastError();
+}
+
 static cudaError_t resolve_big(const HostView& h, int nbig, double dt, cudaStream_t s) {
   if (nbig <= 0) return cudaSuccess;
   k_resolve_big<R, W><<<nbig, 32, 0, s>>>(view_of(h), (R)dt);
@@ -302,6 +315,7 @@ const FormOps CZ_FORM_OBJ = {sizeof(CZ_R),
                              CZ_FORM_NS::prepare,
                              CZ_FORM_NS::integrate,
                              CZ_FORM_NS::narrowphase,
+                             CZ_FORM_NS::collide,
                              CZ_FORM_NS::resolve_big,
                              CZ_FORM_NS::resolve,
                              CZ_FORM_NS::upload,

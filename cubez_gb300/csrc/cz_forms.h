@@ -75,6 +75,9 @@ struct FormOps {
   cudaError_t (*prepare)(size_t np_smem, size_t rs_smem, int lanes);  // function attributes
   cudaError_t (*integrate)(const HostView& v, double dt, double sleep_bias, int threads, cudaStream_t s);
   cudaError_t (*narrowphase)(const HostView& v, int nbs, int threads, int grid, size_t smem, cudaStream_t s);
+  // the narrowphase over a list of units (int2: body, other body or -1 = half-space) of one world
+  cudaError_t (*collide)(const HostView& v, int world, const void* units, int nunits, int nbs, size_t smem,
+                         cudaStream_t s);
   cudaError_t (*resolve_big)(const HostView& v, int nbig, double dt, cudaStream_t s);
   cudaError_t (*resolve)(const HostView& v, int nbs, int cs, int lanes, int grid, size_t smem, double dt,
                          cudaStream_t s);

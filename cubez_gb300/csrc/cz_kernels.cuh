@@ -479,6 +479,83 @@ template <class R> __host__ __device__ inline size_t np_smem_bytes(int nbs) {
   return b;
 }
 
+// Collider transforms (SetAsTransform x identity Offset) and the float32
+// cull data of the staged bodies of one world, by the whole CTA.
+template <class R> __device__ __forceinline__ void np_build_tile(const NPTile<R>& tl, int n) {
+  const int nbs = tl.nbs;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    v3<R> p = V<R>(tl.s(0, i), tl.s(1, i), tl.s(2, i));
+    q4<R> q{tl.s(3, i), tl.s(4, i), tl.s(5, i), tl.s(6, i)};
+    xf<R> t = collider_transform(p, q);
+#pragma unroll
+    for (int r = 0; r < 12; ++r) tl.T[r * nbs + i] = t.m[r];
+    float rb, rl;
+    if (tl.shape[i] == 0) {
+      rb = rl = (float)tl.s(10, i);
+    } else {
+      float hx = (float)tl.s(7, i), hy = (float)tl.s(8, i), hz = (float)tl.s(9, i);
+      rb = sqrtf(hx * hx + hy * hy + hz * hz) * 1.0001f;
+      rl = (hx + hy + hz) * 1.0001f;
+    }
+    tl.cull[i] = (float)t.m[9];
+    tl.cull[nbs + i] = (float)t.m[10];
+    tl.cull[2 * nbs + i] = (float)t.m[11];
+    tl.cull[3 * nbs + i] = rb;
+    tl.cull[4 * nbs + i] = rl;
+  }
+}
+
+// Block-wide scan of one chunk's per-unit contact counts in unit order: the
+// thread's exclusive offset and the chunk total.  The warp totals are
+// double-buffered (scan[32 * parity]), so a chunk needs two barriers.
+__device__ __forceinline__ void np_chunk_scan(int cnt, int* scan, int parity, int* excl, int* total) {
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5, nwarps = (blockDim.x + 31) >> 5;
+  int x = cnt;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    int y = __shfl_up_sync(FULL, x, d);
+    if (lane >= d) x += y;
+  }
+  int* wt = scan + 32 * parity;
+  if (lane == 31) wt[wid] = x;
+  __syncthreads();
+  if (wid == 0) {
+    int t = lane < nwarps ? wt[lane] : 0;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      int y = __shfl_up_sync(FULL, t, d);
+      if (lane >= d) t += y;
+    }
+    if (lane < nwarps) wt[lane] = t;
+  }
+  __syncthreads();
+  *excl = (wid > 0 ? wt[wid - 1] : 0) + x - cnt;
+  *total = wt[nwarps - 1];
+}
+
+// Write one unit's contacts (a pair's single contact or a half-space test's
+// 0..8) at slot `off` of the world's contact slab, within its capacity.
+template <class R>
+__device__ __forceinline__ void np_emit(const NPTile<R>& tl, const BatchView<R>& v, long long cs, int cap, int off,
+                                        int cnt, int i, bool plane, const NPContact<R>& c) {
+  if (cnt <= 0) return;
+  const int room = cap - off;
+  if (room <= 0) return;
+  R* o = v.contact + cs + off;
+  int* ob = v.contact_bodies + cs + off;
+  if (plane) {
+    plane_contacts<R>(tl, i, v, o, ob, v.nc_total, room);
+  } else {
+    const long long S = v.nc_total;
+    o[C_PX * S] = c.px; o[C_PY * S] = c.py; o[C_PZ * S] = c.pz;
+    o[C_NX * S] = c.nx; o[C_NY * S] = c.ny; o[C_NZ * S] = c.nz;
+    o[C_PEN * S] = c.pen;
+    o[C_FRIC * S] = (R)0.9;
+    o[C_REST * S] = (R)0.1;
+    ob[0] = pack_bodies(c.b0, c.b1);
+  }
+}
+
 template <class R>
 __global__ void __launch_bounds__(256) k_narrowphase(BatchView<R> v, int nbs) {
   extern __shared__ __align__(128) unsigned char smem[];
@@ -535,27 +612,7 @@ __global__ void __launch_bounds__(256) k_narrowphase(BatchView<R> v, int nbs) {
         return;
       }
     }
-    // collider transforms + bounding data
-    for (int i = tid; i < n; i += blockDim.x) {
-      v3<R> p = V<R>(tl.s(0, i), tl.s(1, i), tl.s(2, i));
-      q4<R> q{tl.s(3, i), tl.s(4, i), tl.s(5, i), tl.s(6, i)};
-      xf<R> t = collider_transform(p, q);
-#pragma unroll
-      for (int r = 0; r < 12; ++r) tl.T[r * nbs + i] = t.m[r];
-      float rb, rl;
-      if (tl.shape[i] == 0) {
-        rb = rl = (float)tl.s(10, i);
-      } else {
-        float hx = (float)tl.s(7, i), hy = (float)tl.s(8, i), hz = (float)tl.s(9, i);
-        rb = sqrtf(hx * hx + hy * hy + hz * hz) * 1.0001f;
-        rl = (hx + hy + hz) * 1.0001f;
-      }
-      tl.cull[i] = (float)t.m[9];
-      tl.cull[nbs + i] = (float)t.m[10];
-      tl.cull[2 * nbs + i] = (float)t.m[11];
-      tl.cull[3 * nbs + i] = rb;
-      tl.cull[4 * nbs + i] = rl;
-    }
+    np_build_tile(tl, n);
     __syncthreads();
     const long long cs = v.contact_start[w];
     const int cap = v.contact_cap[w];
@@ -577,48 +634,10 @@ __global__ void __launch_bounds__(256) k_narrowphase(BatchView<R> v, int nbs) {
           cnt = pair_test<R>(tl, i, j, v, bstart, c, err);
         }
       }
-      // block-wide inclusive scan of the counts in unit order
-      int x = cnt;
-#pragma unroll
-      for (int d = 1; d < 32; d <<= 1) {
-        int y = __shfl_up_sync(FULL, x, d);
-        if (lane >= d) x += y;
-      }
-      int* wt = scan + 32 * chunk_parity;
-      if (lane == 31) wt[wid] = x;
-      __syncthreads();
-      if (wid == 0) {
-        int t = lane < nwarps ? wt[lane] : 0;
-#pragma unroll
-        for (int d = 1; d < 32; d <<= 1) {
-          int y = __shfl_up_sync(FULL, t, d);
-          if (lane >= d) t += y;
-        }
-        if (lane < nwarps) wt[lane] = t;
-      }
-      __syncthreads();
-      const int prefix = wid > 0 ? wt[wid - 1] : 0;
-      const int total = wt[nwarps - 1];
-      const int off = out + prefix + x - cnt;
+      int excl, total;
+      np_chunk_scan(cnt, scan, chunk_parity, &excl, &total);
       chunk_parity ^= 1;
-      if (cnt > 0) {
-        const int room = cap - off;
-        if (room > 0) {
-          R* o = v.contact + cs + off;
-          int* ob = v.contact_bodies + cs + off;
-          if (k == 0) {
-            plane_contacts<R>(tl, i, v, o, ob, v.nc_total, room);
-          } else {
-            const long long S = v.nc_total;
-            o[C_PX * S] = c.px; o[C_PY * S] = c.py; o[C_PZ * S] = c.pz;
-            o[C_NX * S] = c.nx; o[C_NY * S] = c.ny; o[C_NZ * S] = c.nz;
-            o[C_PEN * S] = c.pen;
-            o[C_FRIC * S] = (R)0.9;
-            o[C_REST * S] = (R)0.1;
-            ob[0] = pack_bodies(c.b0, c.b1);
-          }
-        }
-      }
+      np_emit<R>(tl, v, cs, cap, out + excl, cnt, i, k == 0, c);
       out += total;
     }
     if (err) {
@@ -634,6 +653,68 @@ __global__ void __launch_bounds__(256) k_narrowphase(BatchView<R> v, int nbs) {
       }
     }
     __syncthreads();
+  }
+}
+
+// The narrowphase for a caller's list of units of one world (colliders.go:
+// CheckAgainstHalfSpace when j < 0, else CheckForCollisions(i, j)), in the
+// list's order, replacing the world's contact list: one CTA, bodies staged by
+// plain loads, the same tests, scan and emission as k_narrowphase.  Indices
+// are validated by the host.
+template <class R>
+__global__ void __launch_bounds__(256) k_collide(BatchView<R> v, int w, const int2* __restrict__ units, int nunits,
+                                                 int nbs) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  NPTile<R> tl;
+  tl.nbs = nbs;
+  tl.stage = reinterpret_cast<R*>(smem + 16);
+  tl.T = tl.stage + 11 * nbs;
+  tl.shape = reinterpret_cast<int*>(tl.T + 12 * nbs);
+  tl.cull = reinterpret_cast<float*>(tl.shape + nbs);
+  int* scan = reinterpret_cast<int*>(tl.cull + 5 * nbs);
+  const int tid = threadIdx.x;
+  const int n = v.body_count[w];
+  const int bstart = v.body_start[w];
+  for (int i = tid; i < n; i += blockDim.x) {
+#pragma unroll
+    for (int r = 0; r < 11; ++r) tl.stage[r * nbs + i] = v.body[(long long)r * v.nb_pad + bstart + i];
+    tl.shape[i] = v.shape[bstart + i];
+  }
+  __syncthreads();
+  np_build_tile(tl, n);
+  __syncthreads();
+  const long long cs = v.contact_start[w];
+  const int cap = v.contact_cap[w];
+  int out = 0, parity = 0;
+  uint32_t err = 0;
+  for (int base = 0; base < nunits; base += blockDim.x) {
+    const int u = base + tid;
+    int cnt = 0, i = 0;
+    bool plane = false;
+    NPContact<R> c;
+    if (u < nunits) {
+      const int2 un = units[u];
+      i = un.x;
+      plane = un.y < 0;
+      cnt = plane ? plane_contacts<R>(tl, i, v, nullptr, nullptr, 0, 0) : pair_test<R>(tl, i, un.y, v, bstart, c, err);
+    }
+    int excl, total;
+    np_chunk_scan(cnt, scan, parity, &excl, &total);
+    parity ^= 1;
+    np_emit<R>(tl, v, cs, cap, out + excl, cnt, i, plane, c);
+    out += total;
+  }
+  if (err) {
+    atomicOr(&v.world_status[w], err);
+    atomicOr(v.status, err);
+  }
+  if (tid == 0) {
+    v.contact_count[w] = out;
+    atomicAdd(&v.counters[0], (unsigned long long)out);
+    if (out > cap) {
+      atomicOr(&v.world_status[w], ST_CAPACITY);
+      atomicOr(v.status, ST_CAPACITY);
+    }
   }
 }
 

@@ -62,7 +62,7 @@ typedef struct cz_batch_desc {
   int32_t form;                 /* cz_form */
   int32_t num_worlds;
   const int32_t* body_counts;   /* [num_worlds] bodies per world (world-local index < 65535) */
-  int32_t contact_capacity;     /* per world; 0 = worst case 8n + n(n-1) capped at 64n */
+  int32_t contact_capacity;     /* per world; 0 = worst case 8n + n(n-1) capped at max(64n, 4608) */
   double plane[4];              /* the ground CollisionPlane: normal xyz, offset (colliders.go:29-35) */
   int32_t iteration_multiplier; /* ResolveContacts(len(contacts) * k, ...) as examples/cubedrop.go:73; 0 = 4 */
   int32_t max_iterations;       /* > 0: a fixed maxIterations instead of len(contacts) * k */
@@ -191,6 +191,17 @@ int cz_batch_info(cz_batch* batch, int64_t* info /* [9] */);
  *   work overlaps race on it: serialise them. */
 int cz_resolve_contacts_static(int32_t form, int32_t max_iterations, cz_contact* contacts, int32_t ncontacts,
                                double duration, const cz_bodies* bodies, int32_t nbodies, void* stream);
+
+/* The narrowphase for a caller's list of tests in one world, in the list's
+ * order: units[2u], units[2u+1] = (i, j) runs CheckForCollisions(collider i,
+ * collider j) (colliders.go:720-747), and (i, -1) runs collider i's
+ * CheckAgainstHalfSpace against the plane (colliders.go:180-207, 308-366).
+ * Indices are world-local.  `plane` = {nx, ny, nz, offset}, or NULL for the
+ * batch's plane.  The world's contact list is replaced by the contacts of the
+ * tests in order (read them with cz_contact_counts / cz_download_contacts);
+ * the bodies are the uploaded ones.  This is what a caller with its own pair
+ * list (a broadphase, or per-pair calls of the Go API) binds. */
+int cz_collide(cz_batch* batch, int32_t world, const double* plane, const int32_t* units, int32_t nunits);
 
 /* ---- Learned warm start of adjustVelocities (no counterpart in the
  * reference; the precision form's third variant).  A parameter blob is
