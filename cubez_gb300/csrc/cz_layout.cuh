@@ -101,6 +101,8 @@ template <class R> struct BatchView {
   R* contact;           // [C_NROWS][nc_total]
   int* contact_bodies;  // [nc_total]
   R* work;              // [W_NROWS][nc_total]
+  void* kmat;           // [9][nc_total] island type: K of each contact's friction solve
+  R* kdv;               // [3][nc_total]: the friction response's first row
   int* work_bodies;     // [nc_total]
   long long nc_total;
   const int* order;     // narrowphase queue: worlds in decreasing body count

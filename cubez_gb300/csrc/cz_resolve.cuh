@@ -38,6 +38,9 @@ template <class R, class W> struct RCtx {
   long long wst;
   R* jw;          // impulse rows J0..J2 (row stride jst)
   long long jst;
+  W* kw;          // per contact: K of the friction solve, 9 rows (row stride kst)
+  R* kr;          // per contact: the response matrix's first row, 3 rows
+  long long kst;
   const R* gmat;  // friction / restitution rows of the contact list (null: 0.9 / 0.1)
   long long gst;
   R dt;
@@ -45,6 +48,8 @@ template <class R, class W> struct RCtx {
   __device__ __forceinline__ R& Bf(int r, int i) const { return br[r * nbs + i]; }
   __device__ __forceinline__ R& Cf(int f, int k) const { return cw[(long long)f * cst + k]; }
   __device__ __forceinline__ R& J(int c, int k) const { return jw[(long long)c * jst + k]; }
+  __device__ __forceinline__ W& K(int q, int k) const { return kw[(long long)q * kst + k]; }
+  __device__ __forceinline__ R& KD(int q, int k) const { return kr[(long long)q * kst + k]; }
   __device__ __forceinline__ int& WI(int r, int i) const { return wi[(long long)r * wst + i]; }
   __device__ __forceinline__ R& Save(int r, int i) const { return save[(long long)r * wst + i]; }
   __device__ __forceinline__ R& Delta(int r, int i) const { return delta[(long long)r * wst + i]; }
@@ -300,9 +305,10 @@ template <class R> __device__ __forceinline__ m3<R> skew(const v3<R>& v) {  // c
   return m;
 }
 
-// calculateFrictionImpulse, contact.go:533-606 (3x3 inversion and solve in W)
+// The response matrix of calculateFrictionImpulse (contact.go:540-575): the
+// contact-frame velocity change per unit impulse of both bodies, in R.
 template <class R, class W>
-__device__ v3<R> friction_impulse(const RCtx<R, W>& x, int k, int b0, int b1, const m3<R>& C) {
+__device__ __forceinline__ m3<R> friction_response(const RCtx<R, W>& x, int k, int b0, int b1, const m3<R>& C) {
   R inv_mass = x.Bf(18, b0);
   m3<R> itt = skew(x.Cv(W_R0X, k));
   m3<R> dvw = mulm(itt, x.iit(b0));
@@ -323,10 +329,38 @@ __device__ v3<R> friction_impulse(const RCtx<R, W>& x, int k, int b0, int b1, co
   dv.m[0] += inv_mass;
   dv.m[4] += inv_mass;
   dv.m[8] += inv_mass;
+  return dv;
+}
+
+// The matrices of contact k's friction solve for the whole of
+// adjustVelocities: K = Invert(response) in W (contact.go:577-580,
+// matrix.go:125-153) and the response's first row (R).  They depend on the
+// relative positions, the basis, the inverse masses and the bodies' world
+// inverse inertia, none of which adjustVelocities changes, so computing them
+// once, lane-parallel, at the start of the phase gives exactly the values the
+// reference recomputes at every iteration; the sequential chain then only
+// forms K * (desired delta velocity, -vy, -vz).
+template <class R, class W> __device__ __forceinline__ void friction_prepare(const RCtx<R, W>& x, int k) {
+  if (x.friction(k) == (R)0) return;  // calculateFrictionlessImpulse needs neither
+  const int bb = x.cb[k];
+  const m3<R> dv = friction_response(x, k, body0_of(bb), body1_of(bb), x.basis(k));
   m3<W> dv_w;
 #pragma unroll
   for (int q = 0; q < 9; ++q) dv_w.m[q] = (W)dv.m[q];
   const m3<W> K = invert(dv_w);
+#pragma unroll
+  for (int q = 0; q < 9; ++q) x.K(q, k) = K.m[q];
+  x.KD(0, k) = dv.m[0];
+  x.KD(1, k) = dv.m[3];
+  x.KD(2, k) = dv.m[6];
+}
+
+// calculateFrictionImpulse, contact.go:533-606, from the matrices of
+// friction_prepare: the solve in W, then the dynamic-friction correction.
+template <class R, class W> __device__ v3<R> friction_impulse(const RCtx<R, W>& x, int k) {
+  m3<W> K;
+#pragma unroll
+  for (int q = 0; q < 9; ++q) K.m[q] = x.K(q, k);
   const R ddv = x.Cf(W_DDV, k);
   const v3<W> kill = V<W>((W)ddv, (W)-x.Cf(W_CVY, k), (W)-x.Cf(W_CVZ, k));
   v3<R> ic = cvt<R>(mulv(K, kill));
@@ -335,7 +369,7 @@ __device__ v3<R> friction_impulse(const RCtx<R, W>& x, int k, int b0, int b1, co
   if (planar > ic.x * fr) {
     ic.y /= planar;
     ic.z /= planar;
-    ic.x = dv.m[0] + dv.m[3] * fr * ic.y + dv.m[6] * fr * ic.z;
+    ic.x = x.KD(0, k) + x.KD(1, k) * fr * ic.y + x.KD(2, k) * fr * ic.z;
     ic.x = ddv / ic.x;
     ic.y *= fr * ic.x;
     ic.z *= fr * ic.x;
@@ -364,7 +398,7 @@ __device__ void apply_velocity_change(const RCtx<R, W>& x, const BatchView<R>& v
     }
     ic = V<R>(x.Cf(W_DDV, k) / dvel, (R)0, (R)0);
   } else {
-    ic = friction_impulse(x, k, b0, b1, C);
+    ic = friction_impulse(x, k);
   }
   if (LEARN && v.mode == 1) {  // harvest: total impulse applied at this contact
     x.J(0, k) += ic.x;
@@ -448,6 +482,9 @@ __device__ __forceinline__ void bind_contacts(Slot<R, W>& s, const BatchView<R>&
   }
   x.gmat = v.uniform_material ? nullptr : v.contact + (long long)C_FRIC * v.nc_total + cst;
   x.gst = (long long)(C_REST - C_FRIC) * v.nc_total;
+  x.kw = reinterpret_cast<W*>(v.kmat) + cst;
+  x.kr = v.kdv + cst;
+  x.kst = v.nc_total;
 }
 
 // the learned paths' global scratch of the world whose bodies start at bstart
@@ -858,8 +895,11 @@ __global__ void __launch_bounds__(32) k_resolve(BatchView<R> v, int nbs, int cs,
       if (run && ++used >= max_it) run = false;
     }
     const int pos_used = used;
-    // ---------------- learned warm start / harvest set-up
     const bool solve = active && max_it > 0;
+    if (solve)
+      for (int k = gl; k < C; k += G) friction_prepare(x, k);
+    __syncwarp();
+    // ---------------- learned warm start / harvest set-up
     long long hv_base = -1;
     if (LEARN && mode) {
       // per-body aggregates by integer atomics (order-free, deterministic)

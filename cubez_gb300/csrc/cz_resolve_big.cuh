@@ -63,6 +63,9 @@ __global__ void __launch_bounds__(32) k_resolve_big(BatchView<R> v, R dt) {
   x.save = x.delta = x.jw = nullptr;
   x.wi = nullptr;
   x.wst = x.jst = 0;
+  x.kw = reinterpret_cast<W*>(v.kmat) + cst;
+  x.kr = v.kdv + cst;
+  x.kst = v.nc_total;
   const bool active = C > 0 && dt > (R)0;  // ResolveContacts guards, contact.go:210-212
   if (!active) {
     if (lane == 0) {
@@ -157,6 +160,8 @@ __global__ void __launch_bounds__(32) k_resolve_big(BatchView<R> v, R dt) {
     __syncwarp();
     ++pos_used;
   }
+  for (int k = lane; k < C; k += 32) friction_prepare(x, k);
+  __syncwarp();
   // ---------------- adjustVelocities, contact.go:388-445
   int vel_used = 0;
   while (vel_used < max_it) {

@@ -8,7 +8,7 @@
 // For them this entry point resolves one world's contact list with no
 // allocation at all: its scratch is the file-scope array below, reserved with
 // the library's code, of a fixed size stated by kStaticMaxBodies and
-// kStaticMaxContacts (about 1.8 MB).  Every GPU that loads the library holds
+// kStaticMaxContacts (about 2.8 MB).  Every GPU that loads the library holds
 // that array until the process exits.
 //
 // The array holds the world in the resolver's own layout: body rows, contact
@@ -46,7 +46,9 @@ constexpr size_t kOffContact = align256(kOffAwake + kStaticMaxBodies);
 constexpr size_t kOffCBodies = align256(kOffContact + sizeof(double) * cz::C_NROWS * kStaticMaxContacts);
 constexpr size_t kOffWork = align256(kOffCBodies + sizeof(int) * kStaticMaxContacts);
 constexpr size_t kOffWBodies = align256(kOffWork + sizeof(double) * cz::W_NROWS * kStaticMaxContacts);
-constexpr size_t kOffMeta = align256(kOffWBodies + sizeof(int) * kStaticMaxContacts);
+constexpr size_t kOffKmat = align256(kOffWBodies + sizeof(int) * kStaticMaxContacts);
+constexpr size_t kOffKdv = align256(kOffKmat + sizeof(double) * 9 * kStaticMaxContacts);
+constexpr size_t kOffMeta = align256(kOffKdv + sizeof(double) * 3 * kStaticMaxContacts);
 constexpr size_t kScratchBytes = align256(kOffMeta + 256);
 
 static __device__ __align__(256) unsigned char g_static_scratch[kScratchBytes];
@@ -218,6 +220,8 @@ cz::HostView static_view(unsigned char* scratch, int n) {
   v.contact_bodies = reinterpret_cast<int*>(scratch + kOffCBodies);
   v.work = scratch + kOffWork;
   v.work_bodies = reinterpret_cast<int*>(scratch + kOffWBodies);
+  v.kmat = scratch + kOffKmat;
+  v.kdv = scratch + kOffKdv;
   v.nc_total = kStaticMaxContacts;
   v.order = &m->order;
   v.order_rs = &m->order_rs;

@@ -183,7 +183,7 @@ int cz_batch_info(cz_batch* batch, int64_t* info /* [9] */);
  * optional as in cz_upload_bodies).  Results are written back into those
  * arrays, and the call synchronises `stream` (a cudaStream_t; NULL = the
  * legacy default stream) before it returns.
- *   Scratch: a statically reserved device array of about 1.8 MB that every
+ *   Scratch: a statically reserved device array of about 2.8 MB that every
  *   GPU loading the library holds until exit; hence the limits of at most 64
  *   bodies and 8192 contacts (CZ_ERR_BAD_ARG beyond).  The first call on a
  *   device looks up the array's device address (set-up); make that first call
