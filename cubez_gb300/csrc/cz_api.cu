@@ -132,6 +132,8 @@ struct cz_batch {
   int* ws_int = nullptr;
   uint8_t* ws_u8 = nullptr;
   uint8_t* ws_world = nullptr;
+  float* ws_feat = nullptr;  // harvest features, allocated by the first cz_harvest
+  int wf_grid = 1;           // k_warm_features CTAs
   size_t np_smem = 0, rs_smem = 0;
 
   // graph cache: (nsteps, dt) -> executable graph
@@ -191,6 +193,7 @@ struct cz_batch {
     v.ws_int = ws_int;
     v.ws_u8 = ws_u8;
     v.ws_world = ws_world;
+    v.ws_feat = ws_feat;
     v.big_list = d_big;
     v.big_count = (int)big_ids.size();
     v.big_bw = big_bw;
@@ -262,7 +265,7 @@ void free_batch(cz_batch* b) {
     cudaGraphExecDestroy(kv.second.exec);
     for (cudaEvent_t e : kv.second.ev) cudaEventDestroy(e);
   }
-  void* dev[] = {b->d_units, b->d_big, b->big_bw, b->big_br, b->big_aw, b->big_off, b->big_cnt, b->big_adj, b->ws_rows, b->ws_int, b->ws_u8, b->ws_world, b->mlp_mem, b->hv_features, b->hv_labels, b->hv_count, b->snap_body, b->snap_u8, b->body, b->awake, b->can_sleep, b->shape, b->d_bstart, b->d_bcount, b->d_ccap, b->d_ccount,
+  void* dev[] = {b->ws_feat, b->d_units, b->d_big, b->big_bw, b->big_br, b->big_aw, b->big_off, b->big_cnt, b->big_adj, b->ws_rows, b->ws_int, b->ws_u8, b->ws_world, b->mlp_mem, b->hv_features, b->hv_labels, b->hv_count, b->snap_body, b->snap_u8, b->body, b->awake, b->can_sleep, b->shape, b->d_bstart, b->d_bcount, b->d_ccap, b->d_ccount,
                  b->d_cstart, b->d_wstatus, b->d_piters, b->d_viters, b->contact, b->cbodies, b->work, b->wbodies, b->kmat, b->kdv,
                  b->d_order, b->d_order_rs, b->d_queue, b->d_status, b->d_counters, b->d_h2p, b->d_stage, b->d_stage_u8, b->d_stage_i32,
                  b->d_cstage, b->d_cstage_b, b->d_pow};
@@ -323,7 +326,8 @@ int ensure_pows(cz_batch* b, double dt) {
 }
 
 int launches_per_step(const cz_batch* b) {
-  return 2 + (b->nsmall > 0 ? 1 + (b->nsmall > 32 / b->rs_lanes ? 1 : 0) : 0) + (b->big_ids.empty() ? 0 : 1);
+  return 2 + (b->nsmall > 0 ? 1 + (b->nsmall > 32 / b->rs_lanes ? 1 : 0) + (b->mode != 0 ? 1 : 0) : 0) +
+         (b->big_ids.empty() ? 0 : 1);
 }
 
 int launch_integrate(cz_batch* b, double dt) {
@@ -342,6 +346,11 @@ int launch_narrowphase(cz_batch* b) {
 // others.
 int launch_resolve_with(cz_batch* b, double dt, const cz::HostView& v, int cs, size_t smem) {
   if (b->nsmall > 0) {
+    if (v.mode != 0) {  // features (and, warm-starting, predictions) ahead of the resolver
+      CZ_CUDA(cudaMemsetAsync(b->d_queue + 2, 0, sizeof(unsigned), b->stream));
+      CZ_CUDA(b->ops->warm_features(v, b->rs_nbs, b->wf_grid, dt, b->stream));
+      g_launches++;
+    }
     CZ_CUDA(cudaMemsetAsync(b->d_queue + 1, 0, sizeof(unsigned), b->stream));
     CZ_CUDA(b->ops->resolve(v, b->rs_nbs, cs, b->rs_lanes, b->rs_grid, smem, dt, b->stream));
     g_launches++;
@@ -373,7 +382,7 @@ int configure(cz_batch* b) {
     return fail(CZ_ERR_BODY_LIMIT, "world too large for the shared-memory tiles");
   CZ_CUDA(b->ops->prepare(b->np_smem, b->rs_smem, b->rs_lanes));
   int npb = 0, rsb = 0;
-  CZ_CUDA(b->ops->occupancy(&npb, b->np_threads, b->np_smem, &rsb, b->rs_smem, b->rs_lanes));
+  CZ_CUDA(b->ops->occupancy(&npb, b->np_threads, b->np_smem, &rsb, b->rs_smem, b->rs_lanes, b->mode));
   npb = std::max(npb, 1);
   rsb = std::max(rsb, 1);
   if (b->rs_ctas_per_sm > 0) rsb = std::min(rsb, b->rs_ctas_per_sm);
@@ -382,6 +391,8 @@ int configure(cz_batch* b) {
   b->rs_grid = (int)std::min<long long>(groups, (long long)rsb * b->sm_count);
   b->np_grid = std::max(b->np_grid, 1);
   b->rs_grid = std::max(b->rs_grid, 1);
+  b->wf_grid = (int)std::min<long long>(std::max(b->nsmall, 1),
+                                        (long long)b->ops->warm_features_blocks(b->rs_nbs) * b->sm_count);
   for (auto& kv : b->graphs) cudaGraphExecDestroy(kv.second);
   b->graphs.clear();
   for (auto& kv : b->timed) {
@@ -1050,6 +1061,7 @@ int cz_harvest(cz_batch* b, int32_t nsteps, double dt, int32_t every, float* fea
   }
   if (!b->hv_count) CZ_CUDA(cudaMalloc((void**)&b->hv_count, sizeof(unsigned long long)));
   if (int st0 = ensure_ws(b)) return st0;
+  if (!b->ws_feat) CZ_CUDA(cudaMalloc((void**)&b->ws_feat, sizeof(float) * cz::MLP_IN * (size_t)b->nc_total));
   CZ_CUDA(cudaMemsetAsync(b->hv_count, 0, sizeof(unsigned long long), b->stream));
   int st = ensure_pows(b, dt);
   if (st) return st;

@@ -57,6 +57,7 @@ static BatchView<R> view_of(const HostView& h) {
   v.ws_int = h.ws_int;
   v.ws_u8 = h.ws_u8;
   v.ws_world = h.ws_world;
+  v.ws_feat = h.ws_feat;
   v.big_list = h.big_list;
   v.big_count = h.big_count;
   v.big_bw = h.big_bw;
@@ -261,6 +262,36 @@ static cudaError_t collide(const HostView& h, int world, const void* units, int 
   return cudaGetLastError();
 }
 
+static cudaError_t warm_features(const HostView& h, int nbs, int grid, double dt, cudaStream_t s) {
+  const size_t smem = wf_smem_bytes<R, W>(nbs);
+  {
+    const void* f = (const void*)k_warm_features<R, W>;
+    cudaFuncAttributes a;
+    cudaError_t e = cudaFuncGetAttributes(&a, f);
+    if (e != cudaSuccess) return e;
+    if ((size_t)a.maxDynamicSharedSizeBytes < smem &&
+        (e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) != cudaSuccess)
+      return e;
+  }
+  k_warm_features<R, W><<<grid, 32 * kWfWarps, smem, s>>>(view_of(h), nbs, (R)dt);
+  return cudaGetLastError();
+}
+
+static int warm_features_blocks(int nbs) {
+  const size_t smem = wf_smem_bytes<R, W>(nbs);
+  const void* f = (const void*)k_warm_features<R, W>;
+  cudaFuncAttributes a;
+  if (cudaFuncGetAttributes(&a, f) != cudaSuccess) return 1;
+  if ((size_t)a.maxDynamicSharedSizeBytes < smem &&
+      cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+    return 1;
+  int blocks = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, k_warm_features<R, W>, 32 * kWfWarps, smem) !=
+      cudaSuccess)
+    return 1;
+  return blocks > 0 ? blocks : 1;
+}
+
 static cudaError_t resolve_big(const HostView& h, int nbig, double dt, cudaStream_t s) {
   if (nbig <= 0) return cudaSuccess;
   k_resolve_big<R, W><<<nbig, 32, 0, s>>>(view_of(h), (R)dt);
@@ -281,10 +312,10 @@ static cudaError_t download(const HostView& h, double* sg, uint8_t* u8, int* i32
   return cudaGetLastError();
 }
 
-static cudaError_t occupancy(int* npb, int np_threads, size_t nps, int* rsb, size_t rss, int lanes) {
+static cudaError_t occupancy(int* npb, int np_threads, size_t nps, int* rsb, size_t rss, int lanes, int mode) {
   cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(npb, k_narrowphase<R>, np_threads, nps);
   if (e != cudaSuccess) return e;
-  const void* f = resolve_fn(lanes);  // the plain kernel; the learned one has the same shared-memory use
+  const void* f = resolve_fn_mode(lanes, mode);  // the instantiation that runs (registers differ)
   if (!f) return cudaErrorInvalidValue;
   return cudaOccupancyMaxActiveBlocksPerMultiprocessor(rsb, f, 32, rss);
 }
@@ -318,6 +349,8 @@ const FormOps CZ_FORM_OBJ = {sizeof(CZ_R),
                              CZ_FORM_NS::integrate,
                              CZ_FORM_NS::narrowphase,
                              CZ_FORM_NS::collide,
+                             CZ_FORM_NS::warm_features,
+                             CZ_FORM_NS::warm_features_blocks,
                              CZ_FORM_NS::resolve_big,
                              CZ_FORM_NS::resolve,
                              CZ_FORM_NS::upload,

@@ -54,6 +54,7 @@ struct HostView {
   int* ws_int;
   uint8_t* ws_u8;
   uint8_t* ws_world;
+  float* ws_feat;
   const int* big_list;
   int big_count;
   void* big_bw;
@@ -80,6 +81,9 @@ struct FormOps {
   // the narrowphase over a list of units (int2: body, other body or -1 = half-space) of one world
   cudaError_t (*collide)(const HostView& v, int world, const void* units, int nunits, int nbs, size_t smem,
                          cudaStream_t s);
+  // the learned paths' features / predictions ahead of the resolver (k_warm_features)
+  cudaError_t (*warm_features)(const HostView& v, int nbs, int grid, double dt, cudaStream_t s);
+  int (*warm_features_blocks)(int nbs);  // resident CTAs per SM
   cudaError_t (*resolve_big)(const HostView& v, int nbig, double dt, cudaStream_t s);
   cudaError_t (*resolve)(const HostView& v, int nbs, int cs, int lanes, int grid, size_t smem, double dt,
                          cudaStream_t s);
@@ -88,7 +92,7 @@ struct FormOps {
   cudaError_t (*download)(const HostView& v, double* stage, uint8_t* u8, int* i32, const int* h2p, int nb,
                           cudaStream_t s);
   cudaError_t (*occupancy)(int* np_blocks, int np_threads, size_t np_smem, int* rs_blocks, size_t rs_smem,
-                           int lanes);
+                           int lanes, int mode);
   // contacts: device rows <-> AoS doubles staging (10 doubles + 2 ints per contact)
   cudaError_t (*contacts_out)(const HostView& v, long long start, int count, double* stage, int* bodies,
                               cudaStream_t s);

@@ -87,8 +87,8 @@ __device__ __forceinline__ void mlp_layer(const unsigned (&a)[KS][4], const __nv
     const unsigned* row = reinterpret_cast<const unsigned*>(W + (8 * j + g) * K);
 #pragma unroll
     for (int s = 0; s < KS; ++s) {
-      const unsigned b0 = __ldg(row + 8 * s + t);
-      const unsigned b1 = __ldg(row + 8 * s + 4 + t);
+      const unsigned b0 = row[8 * s + t];  // global or shared weights
+      const unsigned b1 = row[8 * s + 4 + t];
       mma_bf16_16816(c[j], a[s], b0, b1);
     }
   }

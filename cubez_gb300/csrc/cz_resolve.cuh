@@ -425,6 +425,35 @@ __device__ void apply_velocity_change(const RCtx<R, W>& x, const BatchView<R>& v
 }
 
 
+// A world's body rows from the batch rows into the working rows of x, by the
+// `step` lanes of a group (lane index `first`).
+template <class R, class W>
+__device__ __forceinline__ void load_bodies(const RCtx<R, W>& x, const BatchView<R>& v, long long bstart, int n,
+                                            int first, int step) {
+  const long long S = v.nb_pad;
+  for (int i = first; i < n; i += step) {
+    const long long g = bstart + i;
+    x.P(0, i) = (W)v.body[B_PX * S + g];
+    x.P(1, i) = (W)v.body[B_PY * S + g];
+    x.P(2, i) = (W)v.body[B_PZ * S + g];
+    x.P(3, i) = (W)v.body[B_QW * S + g];
+    x.P(4, i) = (W)v.body[B_QX * S + g];
+    x.P(5, i) = (W)v.body[B_QY * S + g];
+    x.P(6, i) = (W)v.body[B_QZ * S + g];
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+      x.Bf(r, i) = v.body[(B_VX + r) * S + g];
+      x.Bf(3 + r, i) = v.body[(B_RX + r) * S + g];
+      x.Bf(6 + r, i) = v.body[(B_LX + r) * S + g];
+    }
+#pragma unroll
+    for (int r = 0; r < 9; ++r) x.Bf(9 + r, i) = v.body[(B_IW0 + r) * S + g];
+    x.Bf(18, i) = v.body[B_INVM * S + g];
+    x.Bf(19, i) = v.body[B_MOTION * S + g];
+    x.aw[i] = v.awake[g];
+  }
+}
+
 // ---------------------------------------------------------------- world slots
 // Shared memory of one world: body rows (W and R), contact working rows,
 // broadcast scratch, packed bodies, awake flags.  The learned paths keep
@@ -794,7 +823,7 @@ __device__ int velocity_loop(const RCtx<R, W>& x, const BatchView<R>& v, int w, 
 // compiles the plain resolver alone (v.mode is ignored), so the learned
 // paths cost the plain kernel no registers.
 template <class R, class W, int G, bool LEARN>
-__global__ void __launch_bounds__(32) k_resolve(BatchView<R> v, int nbs, int cs, R dt) {
+__global__ void __launch_bounds__(32, LEARN ? 9 : 0) k_resolve(BatchView<R> v, int nbs, int cs, R dt) {
   constexpr int NG = 32 / G;
   extern __shared__ __align__(128) unsigned char smem[];
   const int lane = threadIdx.x;
@@ -836,28 +865,9 @@ __global__ void __launch_bounds__(32) k_resolve(BatchView<R> v, int nbs, int cs,
     bind_contacts(sl, v, C, cs, cst);
     if (LEARN && mode) bind_ws(sl, v, bstart, cst);
     if (active) {
-      for (int i = gl; i < n; i += G) {
-        const long long g = bstart + i;
-        x.P(0, i) = (W)v.body[B_PX * S + g];
-        x.P(1, i) = (W)v.body[B_PY * S + g];
-        x.P(2, i) = (W)v.body[B_PZ * S + g];
-        x.P(3, i) = (W)v.body[B_QW * S + g];
-        x.P(4, i) = (W)v.body[B_QX * S + g];
-        x.P(5, i) = (W)v.body[B_QY * S + g];
-        x.P(6, i) = (W)v.body[B_QZ * S + g];
-#pragma unroll
-        for (int r = 0; r < 3; ++r) {
-          x.Bf(r, i) = v.body[(B_VX + r) * S + g];
-          x.Bf(3 + r, i) = v.body[(B_RX + r) * S + g];
-          x.Bf(6 + r, i) = v.body[(B_LX + r) * S + g];
-        }
-#pragma unroll
-        for (int r = 0; r < 9; ++r) x.Bf(9 + r, i) = v.body[(B_IW0 + r) * S + g];
-        x.Bf(18, i) = v.body[B_INVM * S + g];
-        x.Bf(19, i) = v.body[B_MOTION * S + g];
-        x.aw[i] = v.awake[g];
-        if (mode) sl.aw_pre[i] = x.aw[i];
-      }
+      load_bodies(x, v, bstart, n, gl, G);
+      if (mode)
+        for (int i = gl; i < n; i += G) sl.aw_pre[i] = x.aw[i];
     }
     __syncwarp();
     if (active)
@@ -902,39 +912,20 @@ __global__ void __launch_bounds__(32) k_resolve(BatchView<R> v, int nbs, int cs,
     // ---------------- learned warm start / harvest set-up
     long long hv_base = -1;
     if (LEARN && mode) {
-      // per-body aggregates by integer atomics (order-free, deterministic)
+      // the state before adjustVelocities, for the fallback; the per-body
+      // aggregates and the predicted impulses come from k_warm_features
       for (int i = gl; solve && i < n; i += G) {
-        x.WI(WS_DEG, i) = 0;
-        x.WI(WS_NBB, i) = 0;
-        x.WI(WS_LOAD, i) = 0;
-        x.WI(WS_FIRST, i) = 0x7fffffff;
-        x.WI(WS_LAST, i) = -1;
         sl.aw_pos[i] = x.aw[i];
 #pragma unroll
         for (int r = 0; r < 6; ++r) x.Save(r, i) = x.Bf(r, i);
         x.Save(6, i) = x.Bf(19, i);
       }
-      __syncwarp();
-      for (int k = gl; solve && k < C; k += G) {
-        const int bb = x.cb[k];
-        const int b0 = body0_of(bb), b1 = body1_of(bb);
-        const float dd = (float)x.Cf(W_DDV, k);
-        const int fx = dd > 0.f ? (int)(fminf(dd, 100.f) * kLoadScale + 0.5f) : 0;
-        atomicAdd(&x.WI(WS_DEG, b0), 1);
-        atomicAdd(&x.WI(WS_LOAD, b0), fx);
-        if (b1 >= 0) {
-          atomicAdd(&x.WI(WS_DEG, b1), 1);
-          atomicAdd(&x.WI(WS_LOAD, b1), fx);
-          atomicAdd(&x.WI(WS_NBB, b0), 1);
-          atomicAdd(&x.WI(WS_NBB, b1), 1);
-        } else {
-          atomicMin(&x.WI(WS_FIRST, b0), k);
-          atomicMax(&x.WI(WS_LAST, b0), k);
+      if (mode == 1)  // harvest: the impulse totals start at zero
+        for (int k = gl; solve && k < C; k += G) {
+          x.J(0, k) = (R)0;
+          x.J(1, k) = (R)0;
+          x.J(2, k) = (R)0;
         }
-        x.J(0, k) = (R)0;
-        x.J(1, k) = (R)0;
-        x.J(2, k) = (R)0;
-      }
     }
     __syncwarp();
     if (LEARN && mode == 1) {
@@ -944,49 +935,19 @@ __global__ void __launch_bounds__(32) k_resolve(BatchView<R> v, int nbs, int cs,
       b0 = __shfl_sync(FULL, b0, grp * G);
       if (solve && (long long)(b0 + C) <= v.hv_cap) {
         hv_base = (long long)b0;
-        for (int k = gl; k < C; k += G) contact_features(x, k, v.hv_features + (hv_base + k) * MLP_IN);
+        for (int k = gl; k < C; k += G) {
+          const float* f = v.ws_feat + (cst + k) * MLP_IN;  // written by k_warm_features
+          float* o = v.hv_features + (hv_base + k) * MLP_IN;
+#pragma unroll
+          for (int c = 0; c < MLP_IN; ++c) o[c] = f[c];
+        }
       }
     }
     bool warmed = false;  // this world had a warm-started body
-    // a world whose last solve used all its iterations is solved plainly:
-    // it would likely use them all again and be re-solved
+    // a world whose last solve used more than half its iterations is solved
+    // plainly: it is the kind that exhausts them and is then re-solved
     const bool warm_ok = LEARN && mode == 2 && solve && !v.ws_world[w];
     if (LEARN && mode == 2) {
-      // inference, one 16-contact tile at a time, over the worlds of this warp
-      for (int gi = 0; gi < NG; ++gi) {
-        const int Cg = __shfl_sync(FULL, warm_ok ? C : 0, gi * G);
-        const long long cstg = __shfl_sync(FULL, cst, gi * G);
-        const int bstg = __shfl_sync(FULL, bstart, gi * G);
-        if (Cg == 0) continue;
-        Slot<R, W> sg = make_slot<R, W>(smem + (size_t)gi * slot_bytes, nbs, cs, dt);
-        bind_contacts(sg, v, Cg, cs, cstg);
-        bind_ws(sg, v, bstg, cstg);
-        for (int t0 = 0; t0 < Cg; t0 += 16) {
-          // lanes 0..15 compute one contact's normalised features each; the
-          // tile reaches the MMA fragments and back by shuffles alone
-          unsigned row[16];
-          const int k = t0 + lane;
-          const bool mine = lane < 16 && k < Cg;
-          float f[MLP_IN];
-          if (mine) contact_features(sg.x, k, f);
-#pragma unroll
-          for (int c = 0; c < MLP_K1; c += 2) {
-            float lo = 0.f, hi = 0.f;
-            if (mine && c < MLP_IN) lo = (f[c] - v.mlp.mu[c]) * v.mlp.inv_sigma[c];
-            if (mine && c + 1 < MLP_IN) hi = (f[c + 1] - v.mlp.mu[c + 1]) * v.mlp.inv_sigma[c + 1];
-            row[c / 2] = pack_bf16(lo, hi);
-          }
-          unsigned a[2][4];
-          rows_to_a(row, a);
-          float o[4], y[3];
-          mlp_forward_tile(v.mlp, a, o);
-          out_to_rows(o, y);
-          if (mine) {
-#pragma unroll
-            for (int c = 0; c < 3; ++c) sg.x.J(c, k) = (R)(y[c] * v.mlp.out_scale[c]);
-          }
-        }
-      }
       int nw = 0;
       float ssum = 0.f;
       apply_warm_start<R, W, G>(x, n, C, gl, warm_ok, &nw, &ssum);
@@ -1005,7 +966,7 @@ __global__ void __launch_bounds__(32) k_resolve(BatchView<R> v, int nbs, int cs,
       // all its iterations is solved again by the plain path from the saved
       // state (a world without a warm-started body was solved plainly)
       const bool fb = solve && warmed && used >= max_it;
-      if (solve && gl == 0) v.ws_world[w] = used >= max_it;
+      if (solve && gl == 0) v.ws_world[w] = 2 * used > max_it;
       if (__any_sync(FULL, fb)) {
         if (fb) {
           for (int i = gl; i < n; i += G) {
@@ -1093,4 +1054,182 @@ __global__ void __launch_bounds__(32) k_resolve(BatchView<R> v, int nbs, int cs,
   }
 }
 
+// ---------------------------------------------------------------- k_warm_features
+// Shared-memory copy of the inference weights (fragment layouts of MlpDev).
+constexpr size_t WF_W1 = 0;                       // [64][32] bf16
+constexpr size_t WF_W2 = WF_W1 + 64 * 32 * 2;     // [64][64]
+constexpr size_t WF_W3 = WF_W2 + 64 * 64 * 2;     // [64][64]
+constexpr size_t WF_W4 = WF_W3 + 64 * 64 * 2;     // [8][64]
+constexpr size_t WF_B1 = WF_W4 + 8 * 64 * 2;      // f32 [64]
+constexpr size_t WF_B2 = WF_B1 + 64 * 4;
+constexpr size_t WF_B3 = WF_B2 + 64 * 4;
+constexpr size_t WF_B4 = WF_B3 + 64 * 4;          // [8]
+constexpr size_t WF_MU = WF_B4 + 8 * 4;           // [32]
+constexpr size_t WF_IS = WF_MU + 32 * 4;          // [32]
+constexpr size_t WF_OS = WF_IS + 32 * 4;          // [4]
+constexpr size_t WF_BYTES = WF_OS + 16;
+constexpr int kWfWarps = 4;                       // worlds in flight per CTA
+
+// bytes of one warp's body rows, and of a CTA
+template <class R, class W> __host__ __device__ inline size_t wf_slot_bytes(int nbs) {
+  return ((size_t)7 * nbs * sizeof(W) + (size_t)20 * nbs * sizeof(R) + (size_t)((nbs + 15) & ~15) + 15) & ~(size_t)15;
+}
+template <class R, class W> __host__ __device__ inline size_t wf_smem_bytes(int nbs) {
+  return WF_BYTES + kWfWarps * wf_slot_bytes<R, W>(nbs);
+}
+
+// The learned warm start's features and predictions, ahead of k_resolve and
+// off its sequential path: one warp per world, kWfWarps worlds per CTA, the
+// network's weights staged once per CTA in shared memory.  A warp takes the
+// worlds k_resolve will warm-start (in harvest mode, v.mode == 1: every world
+// it solves), stages the bodies, runs calculateInternals (prepare_contact) into
+// the world's global working rows, accumulates the per-body aggregates
+// (integer atomics: order-free, deterministic) and computes each contact's
+// features; mode 2 predicts the impulses in 16-contact BF16 tensor-core tiles
+// into the impulse rows, mode 1 writes the features to ws_feat for the harvest.
+// Same bodies, contacts and arithmetic as k_resolve's own prepareContacts, so
+// the features describe the state adjustVelocities starts from.
+template <class R, class W>
+__global__ void __launch_bounds__(32 * kWfWarps) k_warm_features(BatchView<R> v, int nbs, R dt) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  // weights: global (v.mlp) -> shared
+  {
+    auto copy = [&](size_t off, const void* src, size_t bytes) {
+      const uint4* s4 = reinterpret_cast<const uint4*>(src);
+      uint4* d4 = reinterpret_cast<uint4*>(smem + off);
+      for (size_t i = tid; i < bytes / 16; i += blockDim.x) d4[i] = s4[i];
+    };
+    if (v.mode == 2) {
+      copy(WF_W1, v.mlp.W1, 64 * 32 * 2);
+      copy(WF_W2, v.mlp.W2, 64 * 64 * 2);
+      copy(WF_W3, v.mlp.W3, 64 * 64 * 2);
+      copy(WF_W4, v.mlp.W4, 8 * 64 * 2);
+      copy(WF_B1, v.mlp.b1, 64 * 4);
+      copy(WF_B2, v.mlp.b2, 64 * 4);
+      copy(WF_B3, v.mlp.b3, 64 * 4);
+      copy(WF_B4, v.mlp.b4, 8 * 4);
+      float* mu = reinterpret_cast<float*>(smem + WF_MU);
+      float* is = reinterpret_cast<float*>(smem + WF_IS);
+      float* os = reinterpret_cast<float*>(smem + WF_OS);
+      for (int c = tid; c < 32; c += blockDim.x) {
+        mu[c] = c < MLP_IN ? v.mlp.mu[c] : 0.f;
+        is[c] = c < MLP_IN ? v.mlp.inv_sigma[c] : 0.f;
+      }
+      for (int c = tid; c < 4; c += blockDim.x) os[c] = c < MLP_OUT ? v.mlp.out_scale[c] : 0.f;
+    }
+  }
+  __syncthreads();
+  MlpDev m;
+  m.W1 = reinterpret_cast<const __nv_bfloat16*>(smem + WF_W1);
+  m.W2 = reinterpret_cast<const __nv_bfloat16*>(smem + WF_W2);
+  m.W3 = reinterpret_cast<const __nv_bfloat16*>(smem + WF_W3);
+  m.W4 = reinterpret_cast<const __nv_bfloat16*>(smem + WF_W4);
+  m.b1 = reinterpret_cast<const float*>(smem + WF_B1);
+  m.b2 = reinterpret_cast<const float*>(smem + WF_B2);
+  m.b3 = reinterpret_cast<const float*>(smem + WF_B3);
+  m.b4 = reinterpret_cast<const float*>(smem + WF_B4);
+  const float* mu = reinterpret_cast<const float*>(smem + WF_MU);
+  const float* isg = reinterpret_cast<const float*>(smem + WF_IS);
+  const float* osc = reinterpret_cast<const float*>(smem + WF_OS);
+  unsigned char* slot = smem + WF_BYTES + (size_t)wid * wf_slot_bytes<R, W>(nbs);
+  RCtx<R, W> x;
+  x.nbs = nbs;
+  x.dt = dt;
+  x.bw = reinterpret_cast<W*>(slot);
+  x.br = reinterpret_cast<R*>(x.bw + 7 * nbs);
+  x.aw = reinterpret_cast<uint8_t*>(x.br + 20 * nbs);
+  x.bc = nullptr;
+  x.save = x.delta = nullptr;
+  x.kw = nullptr;
+  x.kr = nullptr;
+  x.kst = 0;
+  const bool harvest = v.mode == 1;
+  for (;;) {
+    unsigned q = 0;
+    if (lane == 0) q = atomicAdd(&v.queue[2], 1u);
+    q = __shfl_sync(FULL, q, 0);
+    if (q >= (unsigned)v.num_worlds) break;
+    const int w = (int)q;
+    const int n = v.body_count[w];
+    int C = v.contact_count[w];
+    const int cap = v.contact_cap[w];
+    if (C > cap) C = cap;
+    const int max_it = v.max_iterations >= 0 ? v.max_iterations : C * v.iter_mult;
+    // the worlds k_resolve solves, and warm-starts unless solving plainly
+    if (C <= 0 || dt <= (R)0 || n > nbs || max_it <= 0 || (!harvest && v.ws_world[w])) continue;
+    const long long bstart = v.body_start[w];
+    const long long cst = v.contact_start[w];
+    x.cw = v.work + cst;
+    x.cb = v.work_bodies + cst;
+    x.cst = v.nc_total;
+    x.gmat = v.uniform_material ? nullptr : v.contact + (long long)C_FRIC * v.nc_total + cst;
+    x.gst = (long long)(C_REST - C_FRIC) * v.nc_total;
+    x.wi = v.ws_int + bstart;
+    x.wst = v.nb_pad;
+    x.jw = v.work + (long long)W_J0 * v.nc_total + cst;
+    x.jst = v.nc_total;
+    load_bodies(x, v, bstart, n, lane, 32);
+    for (int i = lane; i < n; i += 32) {
+      x.WI(WS_DEG, i) = 0;
+      x.WI(WS_NBB, i) = 0;
+      x.WI(WS_LOAD, i) = 0;
+      x.WI(WS_FIRST, i) = 0x7fffffff;
+      x.WI(WS_LAST, i) = -1;
+    }
+    __syncwarp();
+    for (int k = lane; k < C; k += 32) {
+      prepare_contact(x, v, cst + k, k);
+      const int bb = x.cb[k];
+      const int b0 = body0_of(bb), b1 = body1_of(bb);
+      const float dd = (float)x.Cf(W_DDV, k);
+      const int fx = dd > 0.f ? (int)(fminf(dd, 100.f) * kLoadScale + 0.5f) : 0;
+      atomicAdd(&x.WI(WS_DEG, b0), 1);
+      atomicAdd(&x.WI(WS_LOAD, b0), fx);
+      if (b1 >= 0) {
+        atomicAdd(&x.WI(WS_DEG, b1), 1);
+        atomicAdd(&x.WI(WS_LOAD, b1), fx);
+        atomicAdd(&x.WI(WS_NBB, b0), 1);
+        atomicAdd(&x.WI(WS_NBB, b1), 1);
+      } else {
+        atomicMin(&x.WI(WS_FIRST, b0), k);
+        atomicMax(&x.WI(WS_LAST, b0), k);
+      }
+    }
+    __syncwarp();
+    if (harvest) {
+      for (int k = lane; k < C; k += 32) contact_features(x, k, v.ws_feat + (cst + k) * MLP_IN);
+      __syncwarp();
+      continue;
+    }
+    for (int t0 = 0; t0 < C; t0 += 16) {
+      // lanes 0..15 compute one contact's normalised features each; the tile
+      // reaches the MMA fragments and back by shuffles alone
+      unsigned row[16];
+      const int k = t0 + lane;
+      const bool mine = lane < 16 && k < C;
+      float f[MLP_IN];
+      if (mine) contact_features(x, k, f);
+#pragma unroll
+      for (int c = 0; c < MLP_K1; c += 2) {
+        float lo = 0.f, hi = 0.f;
+        if (mine && c < MLP_IN) lo = (f[c] - mu[c]) * isg[c];
+        if (mine && c + 1 < MLP_IN) hi = (f[c + 1] - mu[c + 1]) * isg[c + 1];
+        row[c / 2] = pack_bf16(lo, hi);
+      }
+      unsigned a[2][4];
+      rows_to_a(row, a);
+      float o[4], y[3];
+      mlp_forward_tile(m, a, o);
+      out_to_rows(o, y);
+      if (mine) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) x.J(c, k) = (R)(y[c] * osc[c]);
+      }
+    }
+    __syncwarp();
+  }
+}
+
 }  // namespace cz
+
