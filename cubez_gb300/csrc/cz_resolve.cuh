@@ -227,38 +227,49 @@ __device__ void derive_asleep(const RCtx<R, W>& x, const BatchView<R>& v, int bs
   x.P(3, body) = (W)q.w; x.P(4, body) = (W)q.x; x.P(5, body) = (W)q.y; x.P(6, body) = (W)q.z;
 }
 
-// applyPositionChange, contact.go:285-386 (group leader); the linear and
-// angular changes of both bodies go to x.bc[0..11].
-template <class R, class W>
-__device__ void apply_position_change(const RCtx<R, W>& x, const BatchView<R>& v, int bstart, int k, R penetration) {
-  const int bb = x.cb[k];
-  const int body[2] = {body0_of(bb), body1_of(bb)};
-  const v3<R> n = x.Cv(W_NX, k);
-  const v3<R> rp[2] = {x.Cv(W_R0X, k), x.Cv(W_R1X, k)};
-  R angI[2] = {(R)0, (R)0}, linI[2] = {(R)0, (R)0};
-  R total = (R)0;
-#pragma unroll
-  for (int i = 0; i < 2; ++i) {
-    if (body[i] < 0) continue;
-    v3<R> a = cross(rp[i], n);
-    a = mulv(x.iit(body[i]), a);
-    a = cross(a, rp[i]);
-    angI[i] = dot(a, n);
-    linI[i] = x.Bf(18, body[i]);
-    total += linI[i] + angI[i];
-  }
-  v3<R> lin[2], ang[2];
+// applyPositionChange, contact.go:285-386, by lanes 0 and 1 of a group with
+// `on` (every lane of the warp calls it): lane i moves body i, so the two
+// bodies' float64 position / quaternion updates run side by side; their
+// inertias meet through a shuffle and the total is summed in the reference's
+// order (body 0, then body 1).  Each body's operations are the one-lane
+// formula's, so results are identical.  Lane i leaves body i's linear and
+// angular change in x.bc[3i..3i+2] and x.bc[6+3i..8+3i].
+template <class R, class W, int G>
+__device__ void apply_position_change(const RCtx<R, W>& x, const BatchView<R>& v, int bstart, int k, bool on, int gl) {
+  const bool mine = on && gl < 2;
   const R z = (R)0;
-  lin[0] = lin[1] = ang[0] = ang[1] = V<R>(z, z, z);
-#pragma unroll
-  for (int i = 0; i < 2; ++i) {
-    if (body[i] < 0) continue;
-    const int b = body[i];
-    const R sign = i != 0 ? (R)-1 : (R)1;
-    R am = sign * penetration * (angI[i] / total);
-    R lm = sign * penetration * (linI[i] / total);
-    v3<R> proj = rp[i];
-    add_scaled(proj, n, -dot(rp[i], n));
+  int b = -1;
+  v3<R> n = V<R>(z, z, z), rp = V<R>(z, z, z);
+  R angI = z, linI = z, penetration = z;
+  if (mine) {
+    const int bb = x.cb[k];
+    b = gl == 0 ? body0_of(bb) : body1_of(bb);
+    n = x.Cv(W_NX, k);
+    rp = gl == 0 ? x.Cv(W_R0X, k) : x.Cv(W_R1X, k);
+    penetration = x.Cf(W_PEN, k);
+    if (b >= 0) {
+      v3<R> a = cross(rp, n);
+      a = mulv(x.iit(b), a);
+      a = cross(a, rp);
+      angI = dot(a, n);
+      linI = x.Bf(18, b);
+    }
+  }
+  const R angO = __shfl_sync(0xffffffffu, angI, gl ^ 1, G);
+  const R linO = __shfl_sync(0xffffffffu, linI, gl ^ 1, G);
+  const int bO = __shfl_sync(0xffffffffu, b, gl ^ 1, G);
+  if (!mine) return;
+  const int b0 = gl == 0 ? b : bO, b1 = gl == 0 ? bO : b;
+  R total = z;
+  if (b0 >= 0) total += (gl == 0 ? linI : linO) + (gl == 0 ? angI : angO);
+  if (b1 >= 0) total += (gl == 0 ? linO : linI) + (gl == 0 ? angO : angI);
+  v3<R> lin = V<R>(z, z, z), ang = V<R>(z, z, z);
+  if (b >= 0) {
+    const R sign = gl != 0 ? (R)-1 : (R)1;
+    R am = sign * penetration * (angI / total);
+    R lm = sign * penetration * (linI / total);
+    v3<R> proj = rp;
+    add_scaled(proj, n, -dot(rp, n));
     const R maxm = (R)0.2 * mag(proj);
     if (am < -maxm) {
       R tm = am + lm;
@@ -269,20 +280,18 @@ __device__ void apply_position_change(const RCtx<R, W>& x, const BatchView<R>& v
       am = maxm;
       lm = tm - am;
     }
-    if (am == (R)0) {
-      ang[i] = V<R>(z, z, z);
-    } else {
-      ang[i] = mulv(x.iit(b), cross(rp[i], n));
-      mul_with(ang[i], am / angI[i]);
+    if (am != (R)0) {
+      ang = mulv(x.iit(b), cross(rp, n));
+      mul_with(ang, am / angI);
     }
-    lin[i] = n;
-    mul_with(lin[i], lm);
+    lin = n;
+    mul_with(lin, lm);
     // Position.AddScaled(normal, linearMove): product in R, accumulated in W
     x.P(0, b) += (W)(n.x * lm);
     x.P(1, b) += (W)(n.y * lm);
     x.P(2, b) += (W)(n.z * lm);
     q4<W> q{x.P(3, b), x.P(4, b), x.P(5, b), x.P(6, b)};
-    add_scaled_vector(q, cvt<W>(ang[i]), (W)1);
+    add_scaled_vector(q, cvt<W>(ang), (W)1);
     qnormalize(q);
     x.P(3, b) = q.w; x.P(4, b) = q.x; x.P(5, b) = q.y; x.P(6, b) = q.z;
     if (!x.aw[b]) {
@@ -291,10 +300,8 @@ __device__ void apply_position_change(const RCtx<R, W>& x, const BatchView<R>& v
       derive_asleep(x, v, bstart, b);
     }
   }
-  x.bc[0] = lin[0].x; x.bc[1] = lin[0].y; x.bc[2] = lin[0].z;
-  x.bc[3] = lin[1].x; x.bc[4] = lin[1].y; x.bc[5] = lin[1].z;
-  x.bc[6] = ang[0].x; x.bc[7] = ang[0].y; x.bc[8] = ang[0].z;
-  x.bc[9] = ang[1].x; x.bc[10] = ang[1].y; x.bc[11] = ang[1].z;
+  x.bc[3 * gl] = lin.x; x.bc[3 * gl + 1] = lin.y; x.bc[3 * gl + 2] = lin.z;
+  x.bc[6 + 3 * gl] = ang.x; x.bc[7 + 3 * gl] = ang.y; x.bc[8 + 3 * gl] = ang.z;
 }
 
 template <class R> __device__ __forceinline__ m3<R> skew(const v3<R>& v) {  // contact.go:612-616
@@ -891,10 +898,9 @@ __global__ void __launch_bounds__(32, LEARN ? 9 : 0) k_resolve(BatchView<R> v, i
       }
       group_first_max<G>(best, bidx);
       if (best == 0) run = false;
-      if (run && gl == 0) {
-        match_awake(x, x.cb[bidx]);
-        apply_position_change(x, v, bstart, bidx, x.Cf(W_PEN, bidx));
-      }
+      if (run && gl == 0) match_awake(x, x.cb[bidx]);
+      __syncwarp();
+      apply_position_change<R, W, G>(x, v, bstart, bidx, run, gl);
       __syncwarp();
       if (run) {
         const int rb = x.cb[bidx];

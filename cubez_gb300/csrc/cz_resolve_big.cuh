@@ -149,10 +149,9 @@ __global__ void __launch_bounds__(32) k_resolve_big(BatchView<R> v, R dt) {
     }
     group_first_max<32>(best, bidx);
     if (best == 0) break;
-    if (lane == 0) {
-      match_awake(x, x.cb[bidx]);
-      apply_position_change(x, v, bstart, bidx, x.Cf(W_PEN, bidx));
-    }
+    if (lane == 0) match_awake(x, x.cb[bidx]);
+    __syncwarp();
+    apply_position_change<R, W, 32>(x, v, bstart, bidx, true, lane);
     __syncwarp();
     const int rb = x.cb[bidx];
     const int d0 = body0_of(rb), d1 = body1_of(rb);
