@@ -16,7 +16,7 @@ import itertools
 
 DEFAULT_LANES = (4, 8, 16, 32)
 DEFAULT_TILES = (64, 96, 128, 192)
-DEFAULT_NP_THREADS = (64, 128, 256)
+DEFAULT_NP_THREADS = (32, 64, 128, 256)
 
 
 def tune(batch, frames=30, dt=1.0 / 60.0, lanes=DEFAULT_LANES, tiles=DEFAULT_TILES, np_threads=DEFAULT_NP_THREADS,
