@@ -795,18 +795,21 @@ __device__ __forceinline__ void velocity_update(const RCtx<R, W>& x, int k, int 
 template <class R, class W, int G, bool LEARN>
 __device__ int velocity_loop(const RCtx<R, W>& x, const BatchView<R>& v, int w, int C, int gl, int max_it, bool run) {
   int used = 0;
-  while (__any_sync(FULL, run)) {
-    auto best = key_of((R)0, (R)0);
-    int bidx = 0x7fffffff;
-    if (run) {
-      for (int k = gl; k < C; k += G) {
-        const auto key = key_of(x.Cf(W_DDV, k), (R)0.01);
-        if (key > best) {
-          best = key;
-          bidx = k;
-        }
+  // the lane's best key over its contacts (k = gl mod G): scanned once here,
+  // then by the update pass of each iteration, which visits the same contacts
+  // in the same order right after changing them (a contact's desired delta
+  // velocity changes only in its own lane), so the argmax is the same
+  auto best = key_of((R)0, (R)0);
+  int bidx = 0x7fffffff;
+  if (run)
+    for (int k = gl; k < C; k += G) {
+      const auto key = key_of(x.Cf(W_DDV, k), (R)0.01);
+      if (key > best) {
+        best = key;
+        bidx = k;
       }
     }
+  while (__any_sync(FULL, run)) {
     group_first_max<G>(best, bidx);
     if (best == 0) run = false;
     if (run && gl == 0) {
@@ -814,13 +817,24 @@ __device__ int velocity_loop(const RCtx<R, W>& x, const BatchView<R>& v, int w, 
       apply_velocity_change<R, W, LEARN>(x, v, w, bidx);
     }
     __syncwarp();
+    auto nbest = key_of((R)0, (R)0);
+    int nidx = 0x7fffffff;
     if (run) {
       const int rb = x.cb[bidx];
       const int d0 = body0_of(rb), d1 = body1_of(rb);
-      for (int k = gl; k < C; k += G) velocity_update(x, k, d0, d1);
+      for (int k = gl; k < C; k += G) {
+        velocity_update(x, k, d0, d1);
+        const auto key = key_of(x.Cf(W_DDV, k), (R)0.01);
+        if (key > nbest) {
+          nbest = key;
+          nidx = k;
+        }
+      }
     }
     __syncwarp();
     if (run && ++used >= max_it) run = false;
+    best = nbest;
+    bidx = nidx;
   }
   return used;
 }
@@ -884,31 +898,42 @@ __global__ void __launch_bounds__(32, LEARN ? 9 : 0) k_resolve(BatchView<R> v, i
     // ---------------- adjustPositions, contact.go:231-283
     int used = 0;
     bool run = active && max_it > 0;
-    while (__any_sync(FULL, run)) {
-      auto best = key_of((R)0, (R)0);
-      int bidx = 0x7fffffff;
-      if (run) {
-        for (int k = gl; k < C; k += G) {
-          const auto key = key_of(x.Cf(W_PEN, k), (R)0.01);
-          if (key > best) {
-            best = key;
-            bidx = k;
-          }
+    // as in velocity_loop: the update pass also finds the next argmax
+    auto best = key_of((R)0, (R)0);
+    int bidx = 0x7fffffff;
+    if (run)
+      for (int k = gl; k < C; k += G) {
+        const auto key = key_of(x.Cf(W_PEN, k), (R)0.01);
+        if (key > best) {
+          best = key;
+          bidx = k;
         }
       }
+    while (__any_sync(FULL, run)) {
       group_first_max<G>(best, bidx);
       if (best == 0) run = false;
       if (run && gl == 0) match_awake(x, x.cb[bidx]);
       __syncwarp();
       apply_position_change<R, W, G>(x, v, bstart, bidx, run, gl);
       __syncwarp();
+      auto nbest = key_of((R)0, (R)0);
+      int nidx = 0x7fffffff;
       if (run) {
         const int rb = x.cb[bidx];
         const int d0 = body0_of(rb), d1 = body1_of(rb);
-        for (int k = gl; k < C; k += G) penetration_update(x, k, d0, d1);
+        for (int k = gl; k < C; k += G) {
+          penetration_update(x, k, d0, d1);
+          const auto key = key_of(x.Cf(W_PEN, k), (R)0.01);
+          if (key > nbest) {
+            nbest = key;
+            nidx = k;
+          }
+        }
       }
       __syncwarp();
       if (run && ++used >= max_it) run = false;
+      best = nbest;
+      bidx = nidx;
     }
     const int pos_used = used;
     const bool solve = active && max_it > 0;
