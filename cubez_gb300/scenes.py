@@ -127,6 +127,19 @@ class Scene:
         arrays = {k: np.array(getattr(self, k), copy=True) for k in self.FIELDS}
         return Scene(self.counts.copy(), self.plane.copy(), name=self.name, **arrays)
 
+    @staticmethod
+    def concat(parts, counts=None):
+        """The worlds of several scenes (same plane) in one scene; `counts`
+        may insert empty worlds: a list of per-world body counts whose
+        non-zero entries consume the parts' worlds in order."""
+        arrays = {k: np.concatenate([getattr(p, k) for p in parts]) for k in Scene.FIELDS}
+        all_counts = np.concatenate([p.counts for p in parts])
+        if counts is not None:
+            nz = [c for c in counts if c > 0]
+            assert list(all_counts) == nz, "non-zero counts must match the parts' worlds"
+            all_counts = np.asarray(counts, np.int32)
+        return Scene(all_counts, parts[0].plane.copy(), name="concat", **arrays)
+
     def subset(self, worlds):
         """A scene holding only the listed worlds (same bodies, same order)."""
         idx = np.concatenate([np.arange(self.world_slice(w).start, self.world_slice(w).stop) for w in worlds])

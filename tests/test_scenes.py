@@ -76,3 +76,11 @@ def test_subset():
     assert sub.num_worlds == 2
     np.testing.assert_array_equal(sub.position, np.concatenate([s.position[s.world_slice(2)],
                                                                 s.position[s.world_slice(5)]]))
+
+
+def test_concat_with_empty_worlds():
+    parts = [scenes.mixed(num_worlds=1, seed=90 + i, min_bodies=n, max_bodies=n) for i, n in enumerate((3, 4))]
+    s = scenes.Scene.concat(parts, counts=[0, 3, 0, 4])
+    assert list(s.counts) == [0, 3, 0, 4] and s.num_bodies == 7
+    np.testing.assert_array_equal(s.position[s.world_slice(3)], parts[1].position)
+    assert s.world_slice(0) == slice(0, 0)
