@@ -993,7 +993,7 @@ __global__ void __launch_bounds__(32, LEARN ? 9 : 0) k_resolve(BatchView<R> v, i
     used = velocity_loop<R, W, G, LEARN>(x, v, w, C, gl, max_it, solve);
     int vel_used = used;
     if (LEARN && mode == 2) {
-      // the plain resolver stays the judge: a warm-started world that used
+      // the plain resolver has the last word: a warm-started world that used
       // all its iterations is solved again by the plain path from the saved
       // state (a world without a warm-started body was solved plainly)
       const bool fb = solve && warmed && used >= max_it;
