@@ -128,7 +128,7 @@ template <class R> struct BatchView {
   R* ws_rows;            // [13]: saved velocity 0-2, rotation 3-5, motion 6; warm-start change 7-12
   int* ws_int;           // [WS_NINT]
   uint8_t* ws_u8;        // [2]: awake flags at the start of adjustVelocities, at prepareContacts
-  uint8_t* ws_world;     // [num_worlds]: the world's last velocity solve used more than half its iterations
+  uint8_t* ws_world;     // [num_worlds]: the world's last velocity solve used more than a quarter of its iterations
   float* ws_feat;        // [nc_total][18] harvest features (k_warm_features, mode 1)
   // worlds above the shared-memory slot of k_resolve, resolved by k_resolve_big
   const int* big_list;   // [big_count] world ids

@@ -601,9 +601,11 @@ template <int G, class T> __device__ __forceinline__ T group_min(T v) {
   return v;
 }
 
-// The warm start of one world, for its bodies whose contacts are all with
-// the half-space ("grounded" bodies).  A grounded body's contacts depend on
-// that body's velocity alone, so each one is warm-started independently:
+// The warm start of one world, planned by k_warm_features for its bodies
+// whose contacts are all with the half-space ("grounded" bodies), at the state
+// adjustVelocities starts from (adjustPositions changes no velocity).  A
+// grounded body's contacts depend on that body's velocity alone, so each one
+// is warm-started independently:
 //  1. Predictions of its contacts are projected: normal impulse >= 0,
 //     friction inside the cone |J_t| <= friction * J_n.  Contacts of other
 //     bodies get none.
@@ -616,16 +618,15 @@ template <int G, class T> __device__ __forceinline__ T group_min(T v) {
 //     velocity + max(desired delta, 0) + the velocity epsilon), and no
 //     tangential speed may grow beyond max(current, epsilon).  The resolver
 //     only removes approaching velocity, so it could not undo an overshoot.
-//  4. The body takes s times its change; its contacts update their velocity
-//     and desired delta velocity as adjustVelocities does after an impulse
-//     (contact.go:416-445).
-// Every lane of the warp calls it (it synchronises the warp); `on` selects
-// the groups whose world is solved.  Adds this lane's warm-started bodies and
-// the sum of their scales to *nw and *ssum.
-template <class R, class W, int G>
-__device__ void apply_warm_start(const RCtx<R, W>& x, int n, int C, int gl, bool on, int* nw, float* ssum) {
+//  4. The plan: the body's change times s in the delta rows, each contact's
+//     velocity change times its body's s in the impulse rows (zeros where the
+//     warm start does nothing); warm_start_apply adds them.
+// The 32 lanes of a warp plan one world.  Adds this lane's warm-started bodies
+// and the sum of their scales to *nw and *ssum.
+template <class R, class W>
+__device__ void warm_start_plan(const RCtx<R, W>& x, int n, int C, int lane, int* nw, float* ssum) {
   const R z = (R)0, eps = (R)0.01;
-  for (int k = gl; on && k < C; k += G) {
+  for (int k = lane; k < C; k += 32) {
     const int bb = x.cb[k];
     v3<R> J = V<R>(x.J(0, k), x.J(1, k), x.J(2, k));
     if (body1_of(bb) >= 0 || x.WI(WS_NBB, body0_of(bb)) != 0 || !(J.x > z)) J = V<R>(z, z, z);  // also NaN
@@ -642,21 +643,22 @@ __device__ void apply_warm_start(const RCtx<R, W>& x, int n, int C, int gl, bool
     x.J(2, k) = J.z;
   }
   __syncwarp();
-  for (int i = gl; on && i < n; i += G) {
-    const int deg = x.WI(WS_DEG, i);
-    if (x.WI(WS_NBB, i) != 0 || deg == 0) continue;
+  for (int i = lane; i < n; i += 32) {
     v3<R> dvel = V<R>(z, z, z), drot = V<R>(z, z, z);
-    const m3<R> I = x.iit(i);
-    const R invm = x.Bf(18, i);
-    const int first = x.WI(WS_FIRST, i), last = x.WI(WS_LAST, i);
-    const bool run = last - first + 1 == deg;
-    for (int k = run ? first : 0; k <= (run ? last : C - 1); ++k) {
-      if (!run && body0_of(x.cb[k]) != i) continue;
-      const v3<R> J = V<R>(x.J(0, k), x.J(1, k), x.J(2, k));
-      if (J.x == z) continue;
-      const v3<R> imp = mulv(x.basis(k), J);
-      add(drot, mulv(I, cross(x.Cv(W_R0X, k), imp)));
-      add_scaled(dvel, imp, invm);
+    const int deg = x.WI(WS_DEG, i);
+    if (x.WI(WS_NBB, i) == 0 && deg > 0) {
+      const m3<R> I = x.iit(i);
+      const R invm = x.Bf(18, i);
+      const int first = x.WI(WS_FIRST, i), last = x.WI(WS_LAST, i);
+      const bool run = last - first + 1 == deg;
+      for (int k = run ? first : 0; k <= (run ? last : C - 1); ++k) {
+        if (!run && body0_of(x.cb[k]) != i) continue;
+        const v3<R> J = V<R>(x.J(0, k), x.J(1, k), x.J(2, k));
+        if (J.x == z) continue;
+        const v3<R> imp = mulv(x.basis(k), J);
+        add(drot, mulv(I, cross(x.Cv(W_R0X, k), imp)));
+        add_scaled(dvel, imp, invm);
+      }
     }
 #pragma unroll
     for (int r = 0; r < 3; ++r) {
@@ -668,10 +670,15 @@ __device__ void apply_warm_start(const RCtx<R, W>& x, int n, int C, int gl, bool
   __syncwarp();
   // contact velocity change at s = 1 (into the impulse rows) and the largest
   // scale each contact allows; a body's scale is the smallest of its contacts'
-  for (int k = gl; on && k < C; k += G) {
+  for (int k = lane; k < C; k += 32) {
     const int bb = x.cb[k];
     const int b0 = body0_of(bb);
-    if (body1_of(bb) >= 0 || x.WI(WS_NBB, b0) != 0) continue;
+    if (body1_of(bb) >= 0 || x.WI(WS_NBB, b0) != 0) {
+      x.J(0, k) = z;
+      x.J(1, k) = z;
+      x.J(2, k) = z;
+      continue;
+    }
     const m3<R> Ck = x.basis(k);
     const v3<R> dr = V<R>(x.Delta(3, b0), x.Delta(4, b0), x.Delta(5, b0));
     const v3<R> dl = V<R>(x.Delta(0, b0), x.Delta(1, b0), x.Delta(2, b0));
@@ -703,32 +710,59 @@ __device__ void apply_warm_start(const RCtx<R, W>& x, int n, int C, int gl, bool
     if (sf < 1.f) atomicMin(&x.WI(WS_SCALE, b0), __float_as_int(sf));  // non-negative floats order as ints
   }
   __syncwarp();
-  for (int i = gl; on && i < n; i += G) {
-    if (x.WI(WS_NBB, i) != 0 || x.WI(WS_DEG, i) == 0) continue;
+  for (int i = lane; i < n; i += 32) {
     bool moved = false;
 #pragma unroll
     for (int r = 0; r < 6; ++r) moved |= x.Delta(r, i) != z;
-    if (!moved) continue;
     const R sb = (R)__int_as_float(x.WI(WS_SCALE, i));
-    ++*nw;
-    *ssum += (float)sb;
-    if (sb == z) continue;
+    if (moved) {
+      ++*nw;
+      *ssum += (float)sb;
+    }
 #pragma unroll
-    for (int r = 0; r < 6; ++r) x.Bf(r, i) += sb * x.Delta(r, i);
+    for (int r = 0; r < 6; ++r) x.Delta(r, i) = moved && sb != z ? sb * x.Delta(r, i) : z;
   }
   __syncwarp();
-  for (int k = gl; on && k < C; k += G) {
+  for (int k = lane; k < C; k += 32) {
     const int bb = x.cb[k];
     const int b0 = body0_of(bb);
     if (body1_of(bb) >= 0 || x.WI(WS_NBB, b0) != 0) continue;
     const R sb = (R)__int_as_float(x.WI(WS_SCALE, b0));
+#pragma unroll
+    for (int c = 0; c < 3; ++c) x.J(c, k) = x.J(c, k) != z ? sb * x.J(c, k) : z;
+  }
+}
+
+// The planned warm start, applied at the start of adjustVelocities: each body
+// takes its scaled change, each contact its scaled velocity change and a
+// recomputed desired delta velocity, as adjustVelocities does after an
+// impulse (contact.go:416-445).  A body or contact with nothing planned keeps
+// its values bit for bit.  Every lane of the warp calls it (it synchronises
+// the warp); `on` selects the groups warm-starting.  Returns the bodies this
+// lane moved.
+template <class R, class W, int G>
+__device__ int warm_start_apply(const RCtx<R, W>& x, int n, int C, int gl, bool on) {
+  const R z = (R)0;
+  int moved = 0;
+  for (int i = gl; on && i < n; i += G) {
+    bool any = false;
+#pragma unroll
+    for (int r = 0; r < 6; ++r) any |= x.Delta(r, i) != z;
+    if (!any) continue;
+    ++moved;
+#pragma unroll
+    for (int r = 0; r < 6; ++r) x.Bf(r, i) += x.Delta(r, i);
+  }
+  __syncwarp();
+  for (int k = gl; on && k < C; k += G) {
     const v3<R> dcv = V<R>(x.J(0, k), x.J(1, k), x.J(2, k));
-    if (sb == z || (dcv.x == z && dcv.y == z && dcv.z == z)) continue;
+    if (dcv.x == z && dcv.y == z && dcv.z == z) continue;
     v3<R> cv = x.Cv(W_CVX, k);
-    add_scaled(cv, dcv, sb);
+    add(cv, dcv);
     x.setCv(W_CVX, k, cv);
     x.Cf(W_DDV, k) = desired_dv(x, k);
   }
+  return moved;
 }
 
 // adjustPositions' update of contact k after resolving a contact between
@@ -975,19 +1009,14 @@ __global__ void __launch_bounds__(32, LEARN ? 9 : 0) k_resolve(BatchView<R> v, i
       }
     }
     bool warmed = false;  // this world had a warm-started body
-    // a world whose last solve used more than half its iterations is solved
-    // plainly: it is the kind that exhausts them and is then re-solved
+    // a world whose last solve used more than a quarter of its iterations is
+    // solved plainly: hard worlds are the ones that exhaust the budget and are
+    // then re-solved (a re-solve costs a whole solve in lockstep)
     const bool warm_ok = LEARN && mode == 2 && solve && !v.ws_world[w];
     if (LEARN && mode == 2) {
-      int nw = 0;
-      float ssum = 0.f;
-      apply_warm_start<R, W, G>(x, n, C, gl, warm_ok, &nw, &ssum);
+      const int nw = warm_start_apply<R, W, G>(x, n, C, gl, warm_ok);
       __syncwarp();
       warmed = group_sum<G>(nw) > 0;
-      if (nw) {
-        atomicAdd(&v.counters[6], (unsigned long long)((double)ssum * 1e6 + 0.5));
-        atomicAdd(&v.counters[7], (unsigned long long)nw);
-      }
     }
     // ---------------- adjustVelocities, contact.go:388-445
     used = velocity_loop<R, W, G, LEARN>(x, v, w, C, gl, max_it, solve);
@@ -997,7 +1026,7 @@ __global__ void __launch_bounds__(32, LEARN ? 9 : 0) k_resolve(BatchView<R> v, i
       // all its iterations is solved again by the plain path from the saved
       // state (a world without a warm-started body was solved plainly)
       const bool fb = solve && warmed && used >= max_it;
-      if (solve && gl == 0) v.ws_world[w] = 2 * used > max_it;
+      if (solve && gl == 0) v.ws_world[w] = 4 * used > max_it;
       if (__any_sync(FULL, fb)) {
         if (fb) {
           for (int i = gl; i < n; i += G) {
@@ -1200,6 +1229,7 @@ __global__ void __launch_bounds__(32 * kWfWarps) k_warm_features(BatchView<R> v,
     x.wst = v.nb_pad;
     x.jw = v.work + (long long)W_J0 * v.nc_total + cst;
     x.jst = v.nc_total;
+    x.delta = v.ws_rows + 7 * v.nb_pad + bstart;
     load_bodies(x, v, bstart, n, lane, 32);
     for (int i = lane; i < n; i += 32) {
       x.WI(WS_DEG, i) = 0;
@@ -1257,6 +1287,14 @@ __global__ void __launch_bounds__(32 * kWfWarps) k_warm_features(BatchView<R> v,
 #pragma unroll
         for (int c = 0; c < 3; ++c) x.J(c, k) = (R)(y[c] * osc[c]);
       }
+    }
+    __syncwarp();
+    int nw = 0;
+    float ssum = 0.f;
+    warm_start_plan(x, n, C, lane, &nw, &ssum);
+    if (nw) {
+      atomicAdd(&v.counters[6], (unsigned long long)((double)ssum * 1e6 + 0.5));
+      atomicAdd(&v.counters[7], (unsigned long long)nw);
     }
     __syncwarp();
   }
