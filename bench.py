@@ -234,7 +234,8 @@ def run_ours(args):
             # tune on a settled state (half-way through the rollout), untimed
             b.step(frames // 2, DT)
             b.snapshot()
-            cfg, _ = autotune.tune(b, frames=args.tune_frames, dt=DT)
+            cfg, _ = autotune.tune(b, frames=args.tune_frames, dt=DT,
+                                   warm_shifts=(1, 2, 3) if name == "fp32_mlp" else ())
             tuning[name] = cfg
             b.upload(scene)
         b.prepare_rollout(frames, DT)  # damping factors + graph capture, outside any timed region

@@ -4,9 +4,12 @@ Searches, on the caller's own batch and scene state, over
   * resolver lanes per world G (worlds per warp = 32 / G),
   * the resolver's shared-memory contact tile (contacts per world kept on chip),
   * the narrowphase CTA size,
+  * with the learned warm start enabled, optionally the warm-start budget
+    threshold (which worlds are warm-started; it changes which of two valid
+    solutions a world gets, within the resolver's epsilon, and the speed),
 timing a short captured rollout for each candidate with CUDA events, and
-leaves the batch set to the fastest.  Every candidate computes the same bits
-(the parity tests run all lanes settings), so tuning changes only speed.
+leaves the batch set to the fastest.  The launch-shape candidates all compute the same
+bits (the parity tests run all lanes settings), so they change only speed.
 
 The state is restored from the batch snapshot before every trial, so the
 search is reproducible; the snapshot should hold a representative
@@ -20,7 +23,7 @@ DEFAULT_NP_THREADS = (32, 64, 128, 256)
 
 
 def tune(batch, frames=30, dt=1.0 / 60.0, lanes=DEFAULT_LANES, tiles=DEFAULT_TILES, np_threads=DEFAULT_NP_THREADS,
-         repeats=1, log=None):
+         warm_shifts=(), repeats=1, log=None):
     """Returns (best_config, trials); the batch is left at best_config."""
     trials = []
 
@@ -57,6 +60,15 @@ def tune(batch, frames=30, dt=1.0 / 60.0, lanes=DEFAULT_LANES, tiles=DEFAULT_TIL
         if best_ms is None or ph[2] < best_ms:
             best, best_ms = (g, cfg["resolver_contacts"]), ph[2]
     batch.set_tuning(resolver_lanes=best[0], resolver_contacts=best[1])
+    if warm_shifts:
+        best_shift, shift_ms = None, None
+        for sh in warm_shifts:
+            batch.set_tuning(warm_start_budget_shift=sh)
+            ph = measure()
+            trials.append({"warm_start_budget_shift": sh, "resolver_ms": float(ph[2])})
+            if shift_ms is None or ph[2] < shift_ms:
+                best_shift, shift_ms = sh, ph[2]
+        batch.set_tuning(warm_start_budget_shift=best_shift)
     batch.restore()
     cfg = batch.get_tuning()
     return cfg, trials

@@ -134,6 +134,7 @@ struct cz_batch {
   uint8_t* ws_world = nullptr;
   float* ws_feat = nullptr;  // harvest features, allocated by the first cz_harvest
   int wf_grid = 1;           // k_warm_features CTAs
+  int warm_shift = 2;        // warm-start worlds whose last solve used <= max_it >> warm_shift
   size_t np_smem = 0, rs_smem = 0;
 
   // graph cache: (nsteps, dt) -> executable graph
@@ -194,6 +195,7 @@ struct cz_batch {
     v.ws_u8 = ws_u8;
     v.ws_world = ws_world;
     v.ws_feat = ws_feat;
+    v.warm_shift = warm_shift;
     v.big_list = d_big;
     v.big_count = (int)big_ids.size();
     v.big_bw = big_bw;
@@ -602,6 +604,10 @@ int cz_set_tuning(cz_batch* b, const cz_tuning* t) {
       return fail(CZ_ERR_BAD_ARG, "integrate_threads must be a multiple of 32, at most 256");
     b->int_threads = t->integrate_threads;
   }
+  if (t->warm_start_budget_shift > 0) {
+    if (t->warm_start_budget_shift > 8) return fail(CZ_ERR_BAD_ARG, "warm_start_budget_shift must be 1 to 8");
+    b->warm_shift = t->warm_start_budget_shift;
+  }
   return configure(b);
 }
 
@@ -612,6 +618,7 @@ int cz_get_tuning(cz_batch* b, cz_tuning* t) {
   t->resolver_ctas_per_sm = b->rs_grid / std::max(b->sm_count, 1);
   t->integrate_threads = b->int_threads;
   t->resolver_lanes = b->rs_lanes;
+  t->warm_start_budget_shift = b->warm_shift;
   return CZ_OK;
 }
 

@@ -58,6 +58,7 @@ static BatchView<R> view_of(const HostView& h) {
   v.ws_u8 = h.ws_u8;
   v.ws_world = h.ws_world;
   v.ws_feat = h.ws_feat;
+  v.warm_shift = h.warm_shift;
   v.big_list = h.big_list;
   v.big_count = h.big_count;
   v.big_bw = h.big_bw;

@@ -55,6 +55,7 @@ struct HostView {
   uint8_t* ws_u8;
   uint8_t* ws_world;
   float* ws_feat;
+  int warm_shift;
   const int* big_list;
   int big_count;
   void* big_bw;

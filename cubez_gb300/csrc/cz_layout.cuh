@@ -45,19 +45,27 @@ enum BodyRow : int {
 enum ContactRow : int { C_PX, C_PY, C_PZ, C_NX, C_NY, C_NZ, C_PEN, C_FRIC, C_REST, C_NROWS };
 
 // Resolver working set (Contact's private fields, contact.go:38-50).  The
-// third basis column is not stored: calculateContactBasis (contact.go:118-156)
-// derives it from the normal and the second column by the same formulas.
+// third basis column is never stored: calculateContactBasis (contact.go:
+// 118-156) derives it from the normal and the second column by the same
+// formulas.  The second column (W_TY*) is a function of the normal alone and
+// is stored: recomputing it where the basis is used freed three rows of the
+// resolver's shared-memory tile (10 instead of 9 CTAs per SM for the
+// precision form) but cost more on the update path than the occupancy gained
+// (measured: resolve +2.4 %).
 enum WorkRow : int {
   W_PEN, W_DDV,
   W_NX, W_NY, W_NZ,
-  W_TYX, W_TYY, W_TYZ,
   W_R0X, W_R0Y, W_R0Z,
   W_R1X, W_R1Y, W_R1Z,
   W_CVX, W_CVY, W_CVZ,
+  W_TYX, W_TYY, W_TYZ,
   W_J0, W_J1, W_J2,  // contact-frame impulse: predicted (warm start) or applied in total (harvest)
   W_NROWS
 };
-constexpr int W_NROWS_PLAIN = W_J0;  // rows the plain resolver keeps
+// whether the form stores the basis tangent row
+template <class R> __host__ __device__ constexpr bool stores_tangent() { return true; }
+// rows the resolver keeps per contact in its shared-memory tile
+template <class R> __host__ __device__ constexpr int w_rows_kept() { return stores_tangent<R>() ? W_J0 : W_TYX; }
 
 // World status bits (also OR-ed into the batch status word).
 enum : uint32_t {
@@ -128,8 +136,9 @@ template <class R> struct BatchView {
   R* ws_rows;            // [13]: saved velocity 0-2, rotation 3-5, motion 6; warm-start change 7-12
   int* ws_int;           // [WS_NINT]
   uint8_t* ws_u8;        // [2]: awake flags at the start of adjustVelocities, at prepareContacts
-  uint8_t* ws_world;     // [num_worlds]: the world's last velocity solve used more than a quarter of its iterations
+  uint8_t* ws_world;     // [num_worlds]: the world's last velocity solve used more than max_it >> warm_shift
   float* ws_feat;        // [nc_total][18] harvest features (k_warm_features, mode 1)
+  int warm_shift;        // warm-start a world when its last solve used <= max_it >> warm_shift
   // worlds above the shared-memory slot of k_resolve, resolved by k_resolve_big
   const int* big_list;   // [big_count] world ids
   int big_count;

@@ -21,6 +21,17 @@
 
 namespace cz {
 
+// calculateContactBasis's second column, contact.go:114-156: a function of
+// the normal alone.
+template <class R> __device__ __forceinline__ v3<R> contact_tangent(const v3<R>& n) {
+  if (fabs_<R>(n.x) > fabs_<R>(n.y)) {
+    const R s = (R)1 / sqrt_<R>(n.z * n.z + n.x * n.x);
+    return V<R>(n.z * s, (R)0, n.x * -s);
+  }
+  const R s = (R)1 / sqrt_<R>(n.z * n.z + n.y * n.y);
+  return V<R>((R)0, -n.z * s, n.y * s);
+}
+
 template <class R, class W> struct RCtx {
   W* bw;          // [7][nbs]: position xyz, orientation wxyz (island type)
   R* br;          // [20][nbs]: vel 0-2, rot 3-5, lfa 6-8, iitWorld 9-17, invMass 18, motion 19
@@ -69,7 +80,8 @@ template <class R, class W> struct RCtx {
   // contactToWorld: columns normal, tangent y, tangent z; the last is the
   // reference's formula of the first two (contact.go:136-138, 149-151)
   __device__ __forceinline__ m3<R> basis(int k) const {
-    const v3<R> n = Cv(W_NX, k), ty = Cv(W_TYX, k);
+    const v3<R> n = Cv(W_NX, k);
+    const v3<R> ty = stores_tangent<R>() ? Cv(W_TYX, k) : contact_tangent(n);
     m3<R> m;
     m.m[0] = n.x; m.m[1] = n.y; m.m[2] = n.z;
     m.m[3] = ty.x; m.m[4] = ty.y; m.m[5] = ty.z;
@@ -166,18 +178,9 @@ __device__ void prepare_contact(const RCtx<R, W>& x, const BatchView<R>& v, long
     b1 = -1;
     bb = pack_bodies(b0, b1);
   }
-  // calculateContactBasis, contact.go:114-156
-  v3<R> ty;
-  if (fabs_<R>(n.x) > fabs_<R>(n.y)) {
-    R s = (R)1 / sqrt_<R>(n.z * n.z + n.x * n.x);
-    ty = V<R>(n.z * s, (R)0, n.x * -s);
-  } else {
-    R s = (R)1 / sqrt_<R>(n.z * n.z + n.y * n.y);
-    ty = V<R>((R)0, -n.z * s, n.y * s);
-  }
   x.cb[k] = bb;
   x.setCv(W_NX, k, n);
-  x.setCv(W_TYX, k, ty);
+  if (stores_tangent<R>()) x.setCv(W_TYX, k, contact_tangent(n));  // calculateContactBasis
   const m3<R> C = x.basis(k);
   v3<R> rp0 = p;
   sub(rp0, V<R>((R)x.P(0, b0), (R)x.P(1, b0), (R)x.P(2, b0)));
@@ -470,7 +473,7 @@ template <class R, class W> __host__ __device__ inline size_t rs_slot_bytes(int 
   const size_t nb16 = (size_t)((nbs + 15) & ~15);
   size_t b = (size_t)7 * nbs * sizeof(W);
   b += (size_t)20 * nbs * sizeof(R);
-  b += (size_t)W_NROWS_PLAIN * cs * sizeof(R);
+  b += (size_t)w_rows_kept<R>() * cs * sizeof(R);
   b += 16 * sizeof(R);
   b += (size_t)cs * sizeof(int);
   b += nb16;
@@ -494,7 +497,7 @@ __device__ __forceinline__ Slot<R, W> make_slot(unsigned char* base, int nbs, in
   x.bw = reinterpret_cast<W*>(base);
   x.br = reinterpret_cast<R*>(x.bw + 7 * nbs);
   s.cw_s = x.br + 20 * nbs;
-  x.bc = s.cw_s + (size_t)W_NROWS_PLAIN * cs;
+  x.bc = s.cw_s + (size_t)w_rows_kept<R>() * cs;
   s.cb_s = reinterpret_cast<int*>(x.bc + 16);
   x.aw = reinterpret_cast<uint8_t*>(s.cb_s + cs);
   x.save = x.delta = x.jw = nullptr;
@@ -1009,9 +1012,10 @@ __global__ void __launch_bounds__(32, LEARN ? 9 : 0) k_resolve(BatchView<R> v, i
       }
     }
     bool warmed = false;  // this world had a warm-started body
-    // a world whose last solve used more than a quarter of its iterations is
-    // solved plainly: hard worlds are the ones that exhaust the budget and are
-    // then re-solved (a re-solve costs a whole solve in lockstep)
+    // a world whose last solve used more than max_it >> warm_shift iterations
+    // (a quarter by default) is solved plainly: hard worlds are the ones that
+    // exhaust the budget and are then re-solved (a re-solve costs a whole
+    // solve in lockstep)
     const bool warm_ok = LEARN && mode == 2 && solve && !v.ws_world[w];
     if (LEARN && mode == 2) {
       const int nw = warm_start_apply<R, W, G>(x, n, C, gl, warm_ok);
@@ -1026,7 +1030,7 @@ __global__ void __launch_bounds__(32, LEARN ? 9 : 0) k_resolve(BatchView<R> v, i
       // all its iterations is solved again by the plain path from the saved
       // state (a world without a warm-started body was solved plainly)
       const bool fb = solve && warmed && used >= max_it;
-      if (solve && gl == 0) v.ws_world[w] = 4 * used > max_it;
+      if (solve && gl == 0) v.ws_world[w] = ((long long)used << v.warm_shift) > max_it;
       if (__any_sync(FULL, fb)) {
         if (fb) {
           for (int i = gl; i < n; i += G) {

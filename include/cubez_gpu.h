@@ -258,6 +258,9 @@ typedef struct cz_tuning {
   int32_t resolver_ctas_per_sm;/* resident resolver warps per SM */
   int32_t integrate_threads;
   int32_t resolver_lanes;      /* lanes per world in the resolver: 4, 8, 16 or 32 */
+  int32_t warm_start_budget_shift; /* learned warm start: a world is warm-started when its last
+                                      solve used at most max_iterations >> shift iterations
+                                      (1 to 8; default 2) */
 } cz_tuning;
 int cz_set_tuning(cz_batch* batch, const cz_tuning* tuning);
 int cz_get_tuning(cz_batch* batch, cz_tuning* tuning);
