@@ -234,8 +234,7 @@ def run_ours(args):
             # tune on a settled state (half-way through the rollout), untimed
             b.step(frames // 2, DT)
             b.snapshot()
-            cfg, _ = autotune.tune(b, frames=args.tune_frames, dt=DT,
-                                   warm_shifts=(1, 2, 3) if name == "fp32_mlp" else ())
+            cfg, _ = autotune.tune(b, frames=args.tune_frames, dt=DT)
             tuning[name] = cfg
             b.upload(scene)
         b.prepare_rollout(frames, DT)  # damping factors + graph capture, outside any timed region
@@ -357,6 +356,10 @@ def run_ours(args):
         "fp32_plain_over_fp64": (results["fp32"]["value"] / fp64v) if fp64v else None,
         "mlp_over_fp32_plain": r32["value"] / results["fp32"]["value"],
         "warm_start": {"training": train_info,
+                       "policy": "worlds whose previous solve used at most 1/%d of the iteration budget are "
+                                 "warm-started (warm_start_budget_shift %d); the tuner does not change it"
+                                 % (1 << tuning.get("fp32_mlp", {}).get("warm_start_budget_shift", 2),
+                                    tuning.get("fp32_mlp", {}).get("warm_start_budget_shift", 2)),
                        "warm_worlds_per_frame": cnt["warm_worlds"] / (frames * args.steps),
                        "warm_bodies_per_frame": cnt["warm_bodies"] / (frames * args.steps),
                        "mean_scale": cnt["warm_scale_sum"] / max(1, cnt["warm_bodies"]),
