@@ -4,16 +4,22 @@
 // a group the contacts are lane-strided: the argmax is a G-lane butterfly
 // whose tie-break is the reference's first-maximum rule, and the
 // per-iteration update of every contact touching the two resolved bodies is
-// lane-parallel.  The sequential part of an iteration (applyPositionChange /
-// applyVelocityChange with the friction impulse) runs on the group leaders of
-// all groups at once, so each instruction of that chain serves 32 / G worlds:
-// on GB300 a float64 warp instruction costs the same pipe time whatever its
-// active mask, so packing worlds into a warp divides the float64 cost of the
-// plain form and of the precision form's islands by 32 / G.
+// lane-parallel.  The sequential part of an iteration (applyPositionChange
+// on lanes 0 and 1, one body each; applyVelocityChange on the group leader)
+// runs for all groups at once, so each instruction of that chain serves
+// 32 / G worlds: on GB300 a float64 warp instruction costs the same pipe time
+// whatever its active mask, so packing worlds into a warp divides the float64
+// cost of the plain form and of the precision form's islands by 32 / G.  The
+// friction solve's matrices do not change during adjustVelocities and are
+// computed once per contact, off the chain (friction_prepare).
 //
 // Groups of a warp advance in lockstep rounds; a group whose world is done
 // idles until the warp's last world finishes its phase.  Worlds are queued in
 // decreasing cost, so the worlds sharing a warp have similar iteration counts.
+//
+// Also here: k_warm_features (the learned warm start's features, tensor-core
+// inference and plan, launched before k_resolve) and the shared pieces of
+// k_resolve_big (cz_resolve_big.cuh).
 #pragma once
 #include "cz_layout.cuh"
 #include "cz_math.cuh"
@@ -540,28 +546,6 @@ __device__ __forceinline__ void bind_ws(Slot<R, W>& s, const BatchView<R>& v, lo
   s.aw_pre = v.ws_u8 + v.nb_pad + bstart;
 }
 
-// Contact-frame velocity change per unit impulse of the two bodies together:
-// the matrix calculateFrictionImpulse inverts (contact.go:540-575), here in R
-// alone (a network input, not part of the solve).
-template <class R, class W> __device__ m3<R> response_matrix(const RCtx<R, W>& x, int k, int b0, int b1, const m3<R>& C) {
-  R inv_mass = x.Bf(18, b0);
-  m3<R> itt = skew(x.Cv(W_R0X, k));
-  m3<R> dvw = mulm(mulm(itt, x.iit(b0)), itt);
-  if (b1 >= 0) {
-    itt = skew(x.Cv(W_R1X, k));
-    const m3<R> d2 = mulm(mulm(itt, x.iit(b1)), itt);
-#pragma unroll
-    for (int q = 0; q < 9; ++q) dvw.m[q] += d2.m[q];
-    inv_mass += x.Bf(18, b1);
-  }
-  mulm_with(dvw, (R)-1);
-  m3<R> dv = mulm(mulm(transpose(C), dvw), C);
-  dv.m[0] += inv_mass;
-  dv.m[4] += inv_mass;
-  dv.m[8] += inv_mass;
-  return dv;
-}
-
 // The 18 features of a contact at the start of adjustVelocities, all in the
 // contact basis where they are vectors: the number of contacts between body 0
 // and other bodies, a half-space flag, the contact velocity (3), penetration, desired delta
@@ -579,7 +563,7 @@ template <class R, class W> __device__ void contact_features(const RCtx<R, W>& x
   f[2] = (float)cv.x; f[3] = (float)cv.y; f[4] = (float)cv.z;
   f[5] = (float)x.Cf(W_PEN, k);
   f[6] = (float)ddv;
-  const m3<R> K = response_matrix(x, k, b0, b1, x.basis(k));
+  const m3<R> K = friction_response(x, k, b0, b1, x.basis(k));
   f[7] = (float)K.m[0]; f[8] = (float)K.m[4]; f[9] = (float)K.m[8];
   f[10] = (float)K.m[3]; f[11] = (float)K.m[6]; f[12] = (float)K.m[7];
   f[13] = K.m[0] > (R)0 ? (float)(ddv / K.m[0]) : 0.f;
@@ -592,15 +576,6 @@ template <class R, class W> __device__ void contact_features(const RCtx<R, W>& x
 template <int G> __device__ __forceinline__ int group_sum(int v) {
 #pragma unroll
   for (int off = G / 2; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
-  return v;
-}
-
-template <int G, class T> __device__ __forceinline__ T group_min(T v) {
-#pragma unroll
-  for (int off = G / 2; off > 0; off >>= 1) {
-    const T o = __shfl_xor_sync(0xffffffffu, v, off);
-    v = o < v ? o : v;
-  }
   return v;
 }
 
@@ -876,10 +851,11 @@ __device__ int velocity_loop(const RCtx<R, W>& x, const BatchView<R>& v, int w, 
   return used;
 }
 
-// v.mode: 0 plain, 1 harvest (plain, writing features and applied impulses),
-// 2 learned warm start with fallback to the plain solve.  LEARN = false
-// compiles the plain resolver alone (v.mode is ignored), so the learned
-// paths cost the plain kernel no registers.
+// v.mode: 0 plain, 1 harvest (plain, copying k_warm_features' features and
+// writing the applied impulses), 2 learned warm start (applying
+// k_warm_features' plan) with fallback to the plain solve.  LEARN = false
+// compiles the plain resolver alone (v.mode is ignored), so the learned paths
+// cost the plain kernel no registers.
 template <class R, class W, int G, bool LEARN>
 __global__ void __launch_bounds__(32, LEARN ? 9 : 0) k_resolve(BatchView<R> v, int nbs, int cs, R dt) {
   constexpr int NG = 32 / G;
