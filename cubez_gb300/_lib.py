@@ -30,7 +30,7 @@ class BatchDesc(C.Structure):
 
 BODY_FIELDS = ("position", "orientation", "velocity", "rotation", "acceleration", "inverse_inertia", "inverse_mass",
                "linear_damping", "angular_damping", "motion", "is_awake", "can_sleep", "shape", "half_size", "radius",
-               "inverse_inertia_world", "last_frame_acceleration")
+               "inverse_inertia_world", "last_frame_acceleration", "collider_offset")
 
 
 class Bodies(C.Structure):

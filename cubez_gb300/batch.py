@@ -14,7 +14,8 @@ from ._lib import FORM_FP32, FORM_FP64, check  # noqa: F401
 _DT = {"is_awake": np.uint8, "can_sleep": np.uint8, "shape": np.int32}
 _WIDTH = {"position": 3, "orientation": 4, "velocity": 3, "rotation": 3, "acceleration": 3, "inverse_inertia": 9,
           "inverse_mass": 1, "linear_damping": 1, "angular_damping": 1, "motion": 1, "is_awake": 1, "can_sleep": 1,
-          "shape": 1, "half_size": 3, "radius": 1, "inverse_inertia_world": 9, "last_frame_acceleration": 3}
+          "shape": 1, "half_size": 3, "radius": 1, "inverse_inertia_world": 9, "last_frame_acceleration": 3,
+          "collider_offset": 12}
 
 
 def _ptr(a):
@@ -77,6 +78,7 @@ class WorldBatch:
         if scene is not None:
             for k in scene.FIELDS:
                 arrays.setdefault(k, getattr(scene, k))
+            arrays.setdefault("collider_offset", scene.collider_offset)
         keep = {k: np.ascontiguousarray(v, dtype=_DT.get(k, np.float64)) for k, v in arrays.items() if v is not None}
         s = bodies_struct(keep)
         check(self.L.cz_upload_bodies(self.h, C.byref(s)))

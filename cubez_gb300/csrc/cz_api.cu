@@ -103,6 +103,11 @@ struct cz_batch {
   double* d_cstage = nullptr;
   int* d_cstage_b = nullptr;
   double* d_pow = nullptr;
+  // collider Offsets (allocated by the first upload that carries them)
+  void* d_offset = nullptr;       // [12][nb_pad] rows in the form's real type
+  double* d_off_stage = nullptr;  // [n][12]
+  double* h_off_stage = nullptr;  // pinned [n][12]
+  bool has_offset = false;        // the last upload carried Offsets
   // pinned host staging
   double* h_stage = nullptr;
   uint8_t* h_stage_u8 = nullptr;
@@ -156,6 +161,7 @@ struct cz_batch {
     v.awake = awake;
     v.can_sleep = can_sleep;
     v.shape = shape;
+    v.offset = has_offset ? d_offset : nullptr;
     v.nb_pad = nb_pad;
     v.num_worlds = num_worlds;
     v.max_bodies = max_n;
@@ -267,13 +273,13 @@ void free_batch(cz_batch* b) {
     cudaGraphExecDestroy(kv.second.exec);
     for (cudaEvent_t e : kv.second.ev) cudaEventDestroy(e);
   }
-  void* dev[] = {b->ws_feat, b->d_units, b->d_big, b->big_bw, b->big_br, b->big_aw, b->big_off, b->big_cnt, b->big_adj, b->ws_rows, b->ws_int, b->ws_u8, b->ws_world, b->mlp_mem, b->hv_features, b->hv_labels, b->hv_count, b->snap_body, b->snap_u8, b->body, b->awake, b->can_sleep, b->shape, b->d_bstart, b->d_bcount, b->d_ccap, b->d_ccount,
+  void* dev[] = {b->d_offset, b->d_off_stage, b->ws_feat, b->d_units, b->d_big, b->big_bw, b->big_br, b->big_aw, b->big_off, b->big_cnt, b->big_adj, b->ws_rows, b->ws_int, b->ws_u8, b->ws_world, b->mlp_mem, b->hv_features, b->hv_labels, b->hv_count, b->snap_body, b->snap_u8, b->body, b->awake, b->can_sleep, b->shape, b->d_bstart, b->d_bcount, b->d_ccap, b->d_ccount,
                  b->d_cstart, b->d_wstatus, b->d_piters, b->d_viters, b->contact, b->cbodies, b->work, b->wbodies, b->kmat, b->kdv,
                  b->d_order, b->d_order_rs, b->d_queue, b->d_status, b->d_counters, b->d_h2p, b->d_stage, b->d_stage_u8, b->d_stage_i32,
                  b->d_cstage, b->d_cstage_b, b->d_pow};
   for (void* p : dev)
     if (p) cudaFree(p);
-  void* host[] = {b->h_stage, b->h_stage_u8, b->h_stage_i32, b->h_cstage, b->h_cstage_b, b->h_pow, b->h_status};
+  void* host[] = {b->h_off_stage, b->h_stage, b->h_stage_u8, b->h_stage_i32, b->h_cstage, b->h_cstage_b, b->h_pow, b->h_status};
   for (void* p : host)
     if (p) cudaFreeHost(p);
   if (b->stream) cudaStreamDestroy(b->stream);
@@ -372,6 +378,18 @@ int launch_resolve(cz_batch* b, double dt, const cz::HostView* override_view = n
   return launch_resolve_with(b, dt, override_view ? *override_view : b->view(), b->rs_cs, b->rs_smem);
 }
 
+// The captured graphs hold the kernels' parameters (the batch view); drop them
+// whenever those change.
+void drop_graphs(cz_batch* b) {
+  for (auto& kv : b->graphs) cudaGraphExecDestroy(kv.second);
+  b->graphs.clear();
+  for (auto& kv : b->timed) {
+    cudaGraphExecDestroy(kv.second.exec);
+    for (cudaEvent_t e : kv.second.ev) cudaEventDestroy(e);
+  }
+  b->timed.clear();
+}
+
 int configure(cz_batch* b) {
   // resolver shared-memory tile: shrink the contact capacity until it fits
   int cs = std::min<long long>(b->rs_cs, round_up(b->max_cap, 32));
@@ -395,13 +413,7 @@ int configure(cz_batch* b) {
   b->rs_grid = std::max(b->rs_grid, 1);
   b->wf_grid = (int)std::min<long long>(std::max(b->nsmall, 1),
                                         (long long)b->ops->warm_features_blocks(b->rs_nbs) * b->sm_count);
-  for (auto& kv : b->graphs) cudaGraphExecDestroy(kv.second);
-  b->graphs.clear();
-  for (auto& kv : b->timed) {
-    cudaGraphExecDestroy(kv.second.exec);
-    for (cudaEvent_t e : kv.second.ev) cudaEventDestroy(e);
-  }
-  b->timed.clear();
+  drop_graphs(b);
   return CZ_OK;
 }
 
@@ -653,6 +665,23 @@ int cz_upload_bodies(cz_batch* b, const cz_bodies* in) {
   std::memcpy(b->h_stage_u8, in->is_awake, n);
   std::memcpy(b->h_stage_u8 + n, in->can_sleep, n);
   std::memcpy(b->h_stage_i32, in->shape, sizeof(int) * n);
+  const bool has_off = in->collider_offset != nullptr;
+  if (has_off && !b->d_offset) {
+    if (cudaMalloc(&b->d_offset, b->ops->real_size * 12 * std::max<long long>(b->nb_pad, 1)) != cudaSuccess ||
+        cudaMalloc((void**)&b->d_off_stage, sizeof(double) * 12 * n) != cudaSuccess ||
+        cudaMallocHost((void**)&b->h_off_stage, sizeof(double) * 12 * n) != cudaSuccess)
+      return fail(CZ_ERR_CUDA, "cz_upload_bodies: Offset allocation failed");
+    CZ_CUDA(cudaMemsetAsync(b->d_offset, 0, b->ops->real_size * 12 * std::max<long long>(b->nb_pad, 1), b->stream));
+  }
+  if (has_off != b->has_offset) {
+    drop_graphs(b);  // the narrowphase's view changes
+    b->has_offset = has_off;
+  }
+  if (has_off) {
+    std::memcpy(b->h_off_stage, in->collider_offset, sizeof(double) * 12 * n);
+    CZ_CUDA(cudaMemcpyAsync(b->d_off_stage, b->h_off_stage, sizeof(double) * 12 * n, cudaMemcpyHostToDevice,
+                            b->stream));
+  }
   b->lin_damp.assign(in->linear_damping, in->linear_damping + n);
   b->ang_damp.assign(in->angular_damping, in->angular_damping + n);
   b->pow_dt = std::nan("");
@@ -660,7 +689,7 @@ int cz_upload_bodies(cz_batch* b, const cz_bodies* in) {
   CZ_CUDA(cudaMemcpyAsync(b->d_stage_u8, b->h_stage_u8, 2 * n, cudaMemcpyHostToDevice, b->stream));
   CZ_CUDA(cudaMemcpyAsync(b->d_stage_i32, b->h_stage_i32, sizeof(int) * n, cudaMemcpyHostToDevice, b->stream));
   CZ_CUDA(b->ops->upload(b->view(), b->d_stage, b->d_stage_u8, b->d_stage_i32, b->d_h2p, (int)n, has_iw, has_lfa,
-                         b->stream));
+                         has_off ? b->d_off_stage : nullptr, b->stream));
   g_launches++;
   CZ_CUDA(cudaStreamSynchronize(b->stream));
   return CZ_OK;
@@ -671,8 +700,13 @@ int cz_download_bodies(cz_batch* b, cz_bodies* out) {
   CZ_CUDA(cudaSetDevice(b->device));
   const long long n = b->nb;
   if (n == 0) return CZ_OK;
-  CZ_CUDA(b->ops->download(b->view(), b->d_stage, b->d_stage_u8, b->d_stage_i32, b->d_h2p, (int)n, b->stream));
+  const bool want_off = out->collider_offset && b->has_offset;
+  CZ_CUDA(b->ops->download(b->view(), b->d_stage, b->d_stage_u8, b->d_stage_i32, b->d_h2p, (int)n,
+                           want_off ? b->d_off_stage : nullptr, b->stream));
   g_launches++;
+  if (want_off)
+    CZ_CUDA(cudaMemcpyAsync(b->h_off_stage, b->d_off_stage, sizeof(double) * 12 * n, cudaMemcpyDeviceToHost,
+                            b->stream));
   CZ_CUDA(cudaMemcpyAsync(b->h_stage, b->d_stage, sizeof(double) * cz::SG_NDOUBLES * n, cudaMemcpyDeviceToHost,
                           b->stream));
   CZ_CUDA(cudaMemcpyAsync(b->h_stage_u8, b->d_stage_u8, 2 * n, cudaMemcpyDeviceToHost, b->stream));
@@ -698,6 +732,12 @@ int cz_download_bodies(cz_batch* b, cz_bodies* out) {
   if (out->angular_damping) std::memcpy(out->angular_damping, b->ang_damp.data(), sizeof(double) * n);
   if (out->is_awake) std::memcpy(out->is_awake, b->h_stage_u8, n);
   if (out->can_sleep) std::memcpy(out->can_sleep, b->h_stage_u8 + n, n);
+  if (want_off) {
+    std::memcpy(out->collider_offset, b->h_off_stage, sizeof(double) * 12 * n);
+  } else if (out->collider_offset) {
+    static const double id[12] = {1, 0, 0, 0, 1, 0, 0, 0, 1, 0, 0, 0};
+    for (long long h = 0; h < n; ++h) std::memcpy(out->collider_offset + 12 * h, id, sizeof id);
+  }
   if (out->shape) std::memcpy(out->shape, b->h_stage_i32, sizeof(int) * n);
   return CZ_OK;
 }

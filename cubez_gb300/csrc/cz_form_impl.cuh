@@ -16,6 +16,7 @@ static BatchView<R> view_of(const HostView& h) {
   v.awake = h.awake;
   v.can_sleep = h.can_sleep;
   v.shape = h.shape;
+  v.offset = static_cast<const R*>(h.offset);
   v.nb_pad = h.nb_pad;
   v.num_worlds = h.num_worlds;
   v.max_bodies = h.max_bodies;
@@ -73,7 +74,8 @@ static BatchView<R> view_of(const HostView& h) {
 // Host body data (staged AoS doubles) -> device rows, then
 // CalculateDerivedData where no world inertia was given.
 __global__ void k_upload(BatchView<R> v, const double* __restrict__ sg, const uint8_t* __restrict__ u8,
-                         const int* __restrict__ i32, const int* __restrict__ h2p, int nb, int has_iw, int has_lfa) {
+                         const int* __restrict__ i32, const int* __restrict__ h2p, int nb, int has_iw, int has_lfa,
+                         const double* __restrict__ off) {
   const int h = blockIdx.x * blockDim.x + threadIdx.x;
   if (h >= nb) return;
   const long long p = h2p[h];
@@ -115,10 +117,14 @@ __global__ void k_upload(BatchView<R> v, const double* __restrict__ sg, const ui
   v.awake[p] = u8[h];
   v.can_sleep[p] = u8[n + h];
   v.shape[p] = i32[h];
+  if (off && v.offset) {
+    R* o = const_cast<R*>(v.offset) + p;
+    for (int k = 0; k < 12; ++k) o[k * S] = (R)off[12 * h + k];
+  }
 }
 
 __global__ void k_download(BatchView<R> v, double* __restrict__ sg, uint8_t* __restrict__ u8, int* __restrict__ i32,
-                           const int* __restrict__ h2p, int nb) {
+                           const int* __restrict__ h2p, int nb, double* __restrict__ off) {
   const int h = blockIdx.x * blockDim.x + threadIdx.x;
   if (h >= nb) return;
   const long long p = h2p[h];
@@ -147,6 +153,8 @@ __global__ void k_download(BatchView<R> v, double* __restrict__ sg, uint8_t* __r
   u8[h] = v.awake[p];
   u8[n + h] = v.can_sleep[p];
   i32[h] = v.shape[p];
+  if (off && v.offset)
+    for (int k = 0; k < 12; ++k) off[12 * h + k] = (double)v.offset[k * S + p];
 }
 
 __global__ void k_contacts_out(BatchView<R> v, long long start, int count, double* __restrict__ sg,
@@ -300,16 +308,16 @@ static cudaError_t resolve_big(const HostView& h, int nbig, double dt, cudaStrea
 }
 
 static cudaError_t upload(const HostView& h, const double* sg, const uint8_t* u8, const int* i32, const int* h2p,
-                          int nb, int has_iw, int has_lfa, cudaStream_t s) {
+                          int nb, int has_iw, int has_lfa, const double* off, cudaStream_t s) {
   if (nb <= 0) return cudaSuccess;
-  k_upload<<<(nb + 255) / 256, 256, 0, s>>>(view_of(h), sg, u8, i32, h2p, nb, has_iw, has_lfa);
+  k_upload<<<(nb + 255) / 256, 256, 0, s>>>(view_of(h), sg, u8, i32, h2p, nb, has_iw, has_lfa, off);
   return cudaGetLastError();
 }
 
 static cudaError_t download(const HostView& h, double* sg, uint8_t* u8, int* i32, const int* h2p, int nb,
-                            cudaStream_t s) {
+                            double* off, cudaStream_t s) {
   if (nb <= 0) return cudaSuccess;
-  k_download<<<(nb + 255) / 256, 256, 0, s>>>(view_of(h), sg, u8, i32, h2p, nb);
+  k_download<<<(nb + 255) / 256, 256, 0, s>>>(view_of(h), sg, u8, i32, h2p, nb, off);
   return cudaGetLastError();
 }
 

@@ -16,6 +16,7 @@ struct HostView {
   uint8_t* awake;
   uint8_t* can_sleep;
   int32_t* shape;
+  const void* offset;  // [12][nb_pad] collider Offset rows, or null (identity)
   long long nb_pad;
   int num_worlds;
   int max_bodies;
@@ -88,10 +89,12 @@ struct FormOps {
   cudaError_t (*resolve_big)(const HostView& v, int nbig, double dt, cudaStream_t s);
   cudaError_t (*resolve)(const HostView& v, int nbs, int cs, int lanes, int grid, size_t smem, double dt,
                          cudaStream_t s);
+  // `off` ([n][12] doubles, the collider Offsets) may be null; the upload
+  // writes the Offset rows only when both it and v.offset are set
   cudaError_t (*upload)(const HostView& v, const double* stage, const uint8_t* u8, const int* i32, const int* h2p,
-                        int nb, int has_iw, int has_lfa, cudaStream_t s);
+                        int nb, int has_iw, int has_lfa, const double* off, cudaStream_t s);
   cudaError_t (*download)(const HostView& v, double* stage, uint8_t* u8, int* i32, const int* h2p, int nb,
-                          cudaStream_t s);
+                          double* off, cudaStream_t s);
   cudaError_t (*occupancy)(int* np_blocks, int np_threads, size_t np_smem, int* rs_blocks, size_t rs_smem,
                            int lanes, int mode);
   // contacts: device rows <-> AoS doubles staging (10 doubles + 2 ints per contact)

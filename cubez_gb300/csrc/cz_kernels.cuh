@@ -479,19 +479,51 @@ template <class R> __host__ __device__ inline size_t np_smem_bytes(int nbs) {
   return b;
 }
 
-// Collider transforms (SetAsTransform x identity Offset) and the float32
-// cull data of the staged bodies of one world, by the whole CTA.
-template <class R> __device__ __forceinline__ void np_build_tile(const NPTile<R>& tl, int n) {
+// Whether a collider Offset's rotation part is orthonormal to within 1e-5
+// (a reflection included): then the collider transform is an isometry up to
+// rounding and the cube's bounding radii hold.  NaN fails.
+template <class R> __device__ __forceinline__ bool offset_is_rigid(const R (&o)[12]) {
+  bool ok = true;
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int b = a; b < 3; ++b) {
+      const float d = (float)o[3 * a] * (float)o[3 * b] + (float)o[3 * a + 1] * (float)o[3 * b + 1] +
+                      (float)o[3 * a + 2] * (float)o[3 * b + 2];
+      ok = ok && fabsf(d - (a == b ? 1.f : 0.f)) <= 1e-5f;
+    }
+  return ok;
+}
+
+// Collider transforms (SetAsTransform x Offset) and the float32 cull data of
+// the staged bodies of one world, by the whole CTA.  `off` is the world's
+// first body in the Offset rows (row stride `so`), or null for the identity.
+// A cube whose Offset is not rigid gets infinite bounding radii: its pairs are
+// never culled.
+template <class R>
+__device__ __forceinline__ void np_build_tile(const NPTile<R>& tl, int n, const R* __restrict__ off, long long so) {
   const int nbs = tl.nbs;
   for (int i = threadIdx.x; i < n; i += blockDim.x) {
     v3<R> p = V<R>(tl.s(0, i), tl.s(1, i), tl.s(2, i));
     q4<R> q{tl.s(3, i), tl.s(4, i), tl.s(5, i), tl.s(6, i)};
-    xf<R> t = collider_transform(p, q);
+    xf<R> t;
+    bool rigid = true;
+    if (off) {
+      R o[12];
+#pragma unroll
+      for (int r = 0; r < 12; ++r) o[r] = off[r * so + i];
+      t = collider_transform(p, q, o);
+      rigid = offset_is_rigid(o);
+    } else {
+      t = collider_transform(p, q);
+    }
 #pragma unroll
     for (int r = 0; r < 12; ++r) tl.T[r * nbs + i] = t.m[r];
     float rb, rl;
     if (tl.shape[i] == 0) {
       rb = rl = (float)tl.s(10, i);
+    } else if (!rigid) {
+      rb = rl = __int_as_float(0x7f800000);
     } else {
       float hx = (float)tl.s(7, i), hy = (float)tl.s(8, i), hz = (float)tl.s(9, i);
       rb = sqrtf(hx * hx + hy * hy + hz * hz) * 1.0001f;
@@ -612,7 +644,7 @@ __global__ void __launch_bounds__(256) k_narrowphase(BatchView<R> v, int nbs) {
         return;
       }
     }
-    np_build_tile(tl, n);
+    np_build_tile(tl, n, v.offset ? v.offset + bstart : nullptr, v.nb_pad);
     __syncthreads();
     const long long cs = v.contact_start[w];
     const int cap = v.contact_cap[w];
@@ -681,7 +713,7 @@ __global__ void __launch_bounds__(256) k_collide(BatchView<R> v, int w, const in
     tl.shape[i] = v.shape[bstart + i];
   }
   __syncthreads();
-  np_build_tile(tl, n);
+  np_build_tile(tl, n, v.offset ? v.offset + bstart : nullptr, v.nb_pad);
   __syncthreads();
   const long long cs = v.contact_start[w];
   const int cap = v.contact_cap[w];

@@ -95,6 +95,7 @@ template <class R> struct BatchView {
   uint8_t* awake;       // [nb_pad]
   uint8_t* can_sleep;   // [nb_pad]
   int32_t* shape;       // [nb_pad] 0 sphere, 1 cube, -1 padding
+  const R* offset;      // [12][nb_pad] collider Offset (column-major 3x4), null = identity for every body
   long long nb_pad;
   int num_worlds;
   int max_bodies;       // largest world

@@ -181,10 +181,13 @@ template <class R> struct xf {
   __device__ __forceinline__ v3<R> axis(int c) const { return v3<R>{m[c * 3], m[c * 3 + 1], m[c * 3 + 2]}; }
 };
 
-// matrix.go:165-185 SetAsTransform followed by MulMatrix3x4 with the identity
-// Offset (colliders.go:302-304).  The products with 1 and 0 are evaluated, as
-// the reference does, so signed zeros and non-finite values propagate alike.
-template <class R> __device__ __forceinline__ xf<R> collider_transform(const v3<R>& p, const q4<R>& q) {
+// matrix.go:165-185 SetAsTransform followed by MulMatrix3x4 (matrix.go:
+// 198-217) with the collider's Offset o (column-major 3x4; colliders.go:
+// 173-176, 302-304).  The products are all evaluated, as the reference does,
+// so with the identity Offset signed zeros and non-finite values propagate
+// alike.
+template <class R>
+__device__ __forceinline__ xf<R> collider_transform(const v3<R>& p, const q4<R>& q, const R (&o)[12]) {
   R w = q.w, x = q.x, y = q.y, z = q.z;
   R b[12];
   b[0] = (R)1 - (R)2 * y * y - (R)2 * z * z;
@@ -200,15 +203,20 @@ template <class R> __device__ __forceinline__ xf<R> collider_transform(const v3<
   b[10] = p.y;
   b[11] = p.z;
   xf<R> t;
-  const R one = (R)1, zero = (R)0;
 #pragma unroll
   for (int w2 = 0; w2 < 3; ++w2) {
-    t.m[w2] = b[w2] * one + b[3 + w2] * zero + b[6 + w2] * zero;
-    t.m[3 + w2] = b[w2] * zero + b[3 + w2] * one + b[6 + w2] * zero;
-    t.m[6 + w2] = b[w2] * zero + b[3 + w2] * zero + b[6 + w2] * one;
-    t.m[9 + w2] = b[w2] * zero + b[3 + w2] * zero + b[6 + w2] * zero + b[9 + w2];
+    t.m[w2] = b[w2] * o[0] + b[3 + w2] * o[1] + b[6 + w2] * o[2];
+    t.m[3 + w2] = b[w2] * o[3] + b[3 + w2] * o[4] + b[6 + w2] * o[5];
+    t.m[6 + w2] = b[w2] * o[6] + b[3 + w2] * o[7] + b[6 + w2] * o[8];
+    t.m[9 + w2] = b[w2] * o[9] + b[3 + w2] * o[10] + b[6 + w2] * o[11] + b[9 + w2];
   }
   return t;
+}
+// the identity Offset set by NewCollisionCube / NewCollisionSphere
+// (colliders.go:138, 267)
+template <class R> __device__ __forceinline__ xf<R> collider_transform(const v3<R>& p, const q4<R>& q) {
+  const R id[12] = {(R)1, (R)0, (R)0, (R)0, (R)1, (R)0, (R)0, (R)0, (R)1, (R)0, (R)0, (R)0};
+  return collider_transform(p, q, id);
 }
 
 // matrix.go:187-194

@@ -27,6 +27,8 @@ import numpy as np
 
 SPHERE = 0
 CUBE = 1
+# the collider Offset NewCollisionCube / NewCollisionSphere set (colliders.go:138, 267)
+IDENTITY_OFFSET = np.array([1.0, 0.0, 0.0, 0.0, 1.0, 0.0, 0.0, 0.0, 1.0, 0.0, 0.0, 0.0])
 
 _M64 = np.uint64(0xFFFFFFFFFFFFFFFF)
 
@@ -109,7 +111,15 @@ class Scene:
         self.plane = np.ascontiguousarray(plane, dtype=np.float64)
         for name in self.FIELDS:
             setattr(self, name, arrays[name])
+        # [n, 12] collider Offsets (column-major 3x4, colliders.go:44,64); None = the identity
+        self.collider_offset = arrays.get("collider_offset")
         self.name = arrays.get("name", "scene")
+
+    def _optional(self, idx=None):
+        if self.collider_offset is None:
+            return {}
+        off = self.collider_offset if idx is None else self.collider_offset[idx]
+        return {"collider_offset": np.array(off, dtype=np.float64, copy=True)}
 
     @property
     def num_worlds(self):
@@ -125,6 +135,7 @@ class Scene:
 
     def copy(self):
         arrays = {k: np.array(getattr(self, k), copy=True) for k in self.FIELDS}
+        arrays.update(self._optional())
         return Scene(self.counts.copy(), self.plane.copy(), name=self.name, **arrays)
 
     @staticmethod
@@ -133,6 +144,10 @@ class Scene:
         may insert empty worlds: a list of per-world body counts whose
         non-zero entries consume the parts' worlds in order."""
         arrays = {k: np.concatenate([getattr(p, k) for p in parts]) for k in Scene.FIELDS}
+        if any(p.collider_offset is not None for p in parts):
+            arrays["collider_offset"] = np.concatenate([
+                p.collider_offset if p.collider_offset is not None else np.tile(IDENTITY_OFFSET, (p.num_bodies, 1))
+                for p in parts])
         all_counts = np.concatenate([p.counts for p in parts])
         if counts is not None:
             nz = [c for c in counts if c > 0]
@@ -144,6 +159,7 @@ class Scene:
         """A scene holding only the listed worlds (same bodies, same order)."""
         idx = np.concatenate([np.arange(self.world_slice(w).start, self.world_slice(w).stop) for w in worlds])
         arrays = {k: np.ascontiguousarray(getattr(self, k)[idx]) for k in self.FIELDS}
+        arrays.update(self._optional(idx))
         return Scene(self.counts[list(worlds)], self.plane.copy(), name=self.name, **arrays)
 
 
@@ -264,4 +280,103 @@ def piles(num_worlds=256, seed=5, nx=16, nz=16, ny=4, spacing=1.3):
                      "piles")
 
 
-WORKLOADS = {"cubedrop": cubedrop, "mixed": mixed, "precision": precision, "piles": piles}
+def _rotation_columns(q):
+    """The rotation part of Matrix3x4.SetAsTransform (math/matrix.go:167-180)
+    of rows of quaternions (w, x, y, z): column-major rows of 9."""
+    w, x, y, z = q[:, 0], q[:, 1], q[:, 2], q[:, 3]
+    return np.stack([1 - 2 * y * y - 2 * z * z, 2 * x * y + 2 * w * z, 2 * x * z - 2 * w * y,
+                     2 * x * y - 2 * w * z, 1 - 2 * x * x - 2 * z * z, 2 * y * z + 2 * w * x,
+                     2 * x * z + 2 * w * y, 2 * y * z - 2 * w * x, 1 - 2 * x * x - 2 * y * y], axis=1)
+
+
+def offsets(num_worlds=64, bodies=24, seed=9, nonrigid=0.125):
+    """mixed()-type worlds of `bodies` bodies whose colliders carry an Offset
+    (CollisionCube/CollisionSphere.Offset, colliders.go:44,64): a uniform
+    rotation and a translation U[-0.3,0.3]^3.  A fraction `nonrigid` of the
+    Offsets also scale their three axes by U[0.7,1.3] (the reference applies
+    any 3x4 Offset; such a collider is not a rigid image of its box)."""
+    counts = np.full(num_worlds, bodies, np.int32)
+    w, b = _ids(counts)
+    shape = np.where(_u01(seed, w, b, 0) < 0.5, SPHERE, CUBE)
+    half, radius, pos, quat, vel, rot = _mixed_bodies(seed, counts, shape)
+    sc = _assemble(counts, shape, half, radius, pos, quat, vel, rot, "offsets")
+    r = _rotation_columns(_unit_quaternions(seed, w, b, 160))
+    scaled = _u01(seed, w, b, 20) < nonrigid
+    scale = np.stack([_uniform(seed, w, b, 21 + k, 0.7, 1.3) for k in range(3)], axis=1)
+    scale = np.where(scaled[:, None], scale, 1.0)
+    r = r * np.repeat(scale, 3, axis=1)
+    t = np.stack([_uniform(seed, w, b, 24 + k, -0.3, 0.3) for k in range(3)], axis=1)
+    sc.collider_offset = np.ascontiguousarray(np.concatenate([r, t], axis=1))
+    return sc
+
+
+def ballistic(num_worlds=16, bullets=8, seed=13):
+    """The scene of examples/ballistic.go:149-231 as a batch of worlds.
+    Body 0: the cube (half size 1, mass 8, block inertia, at (x0, 5, 0) with
+    x0 ~ U[-0.5, 0.5]).  Body 1: the backboard (half size (0.5, 2, 0.25) at
+    (0, 2, -10), SetInfiniteMass, zero inverse inertia).  Bodies 2..: the
+    bullets of fire() (spheres r = 0.2, mass 1.5, inertia 0.4 m r^2, velocity
+    (0, 0, -40), acceleration (0, -2.5, 0)), bullet k starting at
+    (U[-0.3, 0.3], 1.5 + U[-0.2, 0.2], 20 + 4k).  The cube and bullets keep
+    NewRigidBody's defaults (rigidbody.go:104-114: both dampings 0.95, gravity
+    -9.78 on the cube, CanSleep).
+
+    The example never integrates the backboard.  A batch integrates every
+    body, so the backboard is made static: zero acceleration, velocity and
+    rotation and CanSleep false.  Integrate then leaves its state unchanged
+    bit for bit, and the contact impulses move it by inverse mass and inverse
+    inertia zero, so every frame equals the example's."""
+    n = 2 + bullets
+    counts = np.full(num_worlds, n, np.int32)
+    w, b = _ids(counts)
+    N = len(w)
+    shape = np.where(b < 2, CUBE, SPHERE).astype(np.int32)
+    half = np.zeros((N, 3))
+    half[b == 0] = (1.0, 1.0, 1.0)
+    half[b == 1] = (0.5, 2.0, 0.25)
+    radius = np.where(b >= 2, 0.2, 0.0)
+    pos = np.zeros((N, 3))
+    cube, board, bullet = b == 0, b == 1, b >= 2
+    pos[cube, 0] = _uniform(seed, w[cube], b[cube], 1, -0.5, 0.5)
+    pos[cube, 1] = 5.0
+    pos[board] = (0.0, 2.0, -10.0)
+    k = (b - 2).astype(np.float64)
+    pos[bullet, 0] = _uniform(seed, w[bullet], b[bullet], 2, -0.3, 0.3)
+    pos[bullet, 1] = 1.5 + _uniform(seed, w[bullet], b[bullet], 3, -0.2, 0.2)
+    pos[bullet, 2] = 20.0 + 4.0 * k[bullet]
+    quat = np.tile([1.0, 0.0, 0.0, 0.0], (N, 1))
+    vel = np.zeros((N, 3))
+    vel[bullet, 2] = -40.0
+    acc = np.zeros((N, 3))
+    acc[cube, 1] = -9.78
+    acc[bullet, 1] = -2.5
+    inv_mass = np.where(cube, 1.0 / 8.0, np.where(bullet, 1.0 / 1.5, 0.0))
+    # SetBlockInertiaTensor(h = 1, m = 8) and SetInertiaTensorCoeffs(0.4 m r^2), inverted
+    ic = 0.3 * 8.0 * (1.0 + 1.0)
+    c = ((0.4 * 1.5) * 0.2) * 0.2
+    inertia = np.where(cube[:, None], _coeffs(np.full(N, ic), np.full(N, ic), np.full(N, ic)),
+                       _coeffs(np.full(N, c), np.full(N, c), np.full(N, c)))
+    inv_inertia = _invert3(inertia)
+    inv_inertia[board] = 0.0
+    return Scene(counts, (0.0, 1.0, 0.0, 0.0), name="ballistic", position=pos, orientation=quat, velocity=vel,
+                 rotation=np.zeros((N, 3)), acceleration=acc, inverse_inertia=np.ascontiguousarray(inv_inertia),
+                 inverse_mass=inv_mass, linear_damping=np.full(N, 0.95), angular_damping=np.full(N, 0.95),
+                 motion=np.full(N, 0.3 * 2.0), is_awake=np.ones(N, np.uint8),
+                 can_sleep=np.where(board, 0, 1).astype(np.uint8), shape=shape, half_size=half,
+                 radius=np.ascontiguousarray(radius))
+
+
+def ballistic_units(bodies):
+    """generateContacts of examples/ballistic.go:47-98 as a unit list for a
+    world of `bodies` bodies laid out as ballistic() does: (i, -1) is i's
+    half-space test, (i, j) CheckForCollisions(i, j)."""
+    units = [(0, -1), (0, 1)]
+    bl = range(2, bodies)
+    for k in bl:
+        units += [(k, -1), (0, k), (1, k)]
+        units += [(k2, k) for k2 in bl if k2 != k]
+    return np.asarray(units, np.int32)
+
+
+WORKLOADS = {"cubedrop": cubedrop, "mixed": mixed, "precision": precision, "piles": piles, "offsets": offsets,
+             "ballistic": ballistic}

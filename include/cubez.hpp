@@ -28,8 +28,8 @@
  *  - where the reference panics (a nil body dereference in the frictionless
  *    impulse, a box-box test reaching no axis), a cubez::Error carrying the
  *    cz_status is thrown;
- *  - collider Offset must be the identity (the reference's constructors set
- *    it so and nothing on the path changes it); another Offset throws.
+ *  - a collider's transform (body transform x Offset) is derived where it is
+ *    used, so CalculateDerivedData on a collider has nothing to store.
  *
  * Host-side setup helpers (SetBlockInertiaTensor, Invert, SetAsTransform)
  * compute what the Go setup code computes once per body; they are not on the
@@ -114,6 +114,15 @@ inline Matrix3x4 AsTransform(const Vector3& p, const Quat& q) {
                    p[0],                      p[1],                      p[2]};
 }
 
+// Matrix3x4.MulMatrix3x4, math/matrix.go:196-217
+inline Matrix3x4 MulMatrix3x4(const Matrix3x4& m, const Matrix3x4& o) {
+  Matrix3x4 r;
+  for (int c = 0; c < 3; ++c)
+    for (int i = 0; i < 3; ++i) r[3 * c + i] = m[i] * o[3 * c] + m[3 + i] * o[3 * c + 1] + m[6 + i] * o[3 * c + 2];
+  for (int i = 0; i < 3; ++i) r[9 + i] = m[i] * o[9] + m[3 + i] * o[10] + m[6 + i] * o[11] + m[9 + i];
+  return r;
+}
+
 class RigidBody;
 class CollisionPlane;
 class CollisionSphere;
@@ -169,7 +178,8 @@ class Runtime {
 // Structure-of-arrays staging of a list of bodies for cz_bodies.
 struct Staging {
   std::vector<double> position, orientation, velocity, rotation, acceleration, inverse_inertia, inverse_mass,
-      linear_damping, angular_damping, motion, half_size, radius, iit_world, lfa;
+      linear_damping, angular_damping, motion, half_size, radius, iit_world, lfa, offset;
+  bool has_offset = false;  // some collider's Offset is not the identity
   std::vector<uint8_t> is_awake, can_sleep;
   std::vector<int32_t> shape;
   cz_bodies view() {
@@ -191,6 +201,7 @@ struct Staging {
     b.radius = radius.data();
     b.inverse_inertia_world = iit_world.data();
     b.last_frame_acceleration = lfa.data();
+    b.collider_offset = has_offset ? offset.data() : nullptr;
     return b;
   }
 };
@@ -284,8 +295,8 @@ class Collider {
   virtual ~Collider() = default;
   virtual RigidBody* GetBody() const = 0;
   virtual Matrix3x4 GetTransform() const = 0;
-  // the collider transform is the body transform times the identity Offset;
-  // the GPU derives it where it needs it
+  // the collider transform is the body transform times the Offset
+  // (colliders.go:173-176, 302-304); the GPU derives it where it needs it
   virtual void CalculateDerivedData() {}
   virtual bool CheckAgainstHalfSpace(const CollisionPlane& plane, std::vector<Contact>& contacts) = 0;
   virtual bool CheckAgainstSphere(CollisionSphere& sphere, std::vector<Contact>& contacts) = 0;
@@ -319,7 +330,7 @@ class CollisionSphere : public Collider {
     }
   }
   RigidBody* GetBody() const override { return Body; }
-  Matrix3x4 GetTransform() const override { return Body->GetTransform(); }
+  Matrix3x4 GetTransform() const override;
   bool CheckAgainstHalfSpace(const CollisionPlane& plane, std::vector<Contact>& contacts) override;
   bool CheckAgainstSphere(CollisionSphere& sphere, std::vector<Contact>& contacts) override;
   bool CheckAgainstCube(CollisionCube& cube, std::vector<Contact>& contacts) override;
@@ -341,7 +352,7 @@ class CollisionCube : public Collider {
     }
   }
   RigidBody* GetBody() const override { return Body; }
-  Matrix3x4 GetTransform() const override { return Body->GetTransform(); }
+  Matrix3x4 GetTransform() const override;
   bool CheckAgainstHalfSpace(const CollisionPlane& plane, std::vector<Contact>& contacts) override;
   bool CheckAgainstSphere(CollisionSphere& sphere, std::vector<Contact>& contacts) override;
   bool CheckAgainstCube(CollisionCube& cube, std::vector<Contact>& contacts) override;
@@ -353,7 +364,8 @@ class CollisionCube : public Collider {
 // ---------------------------------------------------------------- marshalling
 struct Marshal {
   // one body (with its collider's shape) into slot k of the staging arrays
-  static void put(gpu::Staging& s, int k, const RigidBody& b, int shape, const Vector3& half, Real radius) {
+  static void put(gpu::Staging& s, int k, const RigidBody& b, int shape, const Vector3& half, Real radius,
+                  const Matrix3x4& offset = Identity3x4()) {
     auto set = [&](std::vector<double>& v, int w, const Real* src) {
       for (int i = 0; i < w; ++i) v[(size_t)k * w + i] = src[i];
     };
@@ -366,6 +378,8 @@ struct Marshal {
     set(s.iit_world, 9, b.iitWorld_.data());
     set(s.lfa, 3, b.lastFrameAccelleration_.data());
     set(s.half_size, 3, half.data());
+    set(s.offset, 12, offset.data());
+    if (offset != Identity3x4()) s.has_offset = true;
     s.inverse_mass[k] = b.inverseMass_;
     s.linear_damping[k] = b.LinearDamping;
     s.angular_damping[k] = b.AngularDamping;
@@ -398,6 +412,11 @@ struct Marshal {
     s.orientation.assign(4 * n, 0);
     s.inverse_inertia.assign(9 * n, 0);
     s.iit_world.assign(9 * n, 0);
+    s.offset.clear();
+    for (int k = 0; k < n; ++k) {
+      const Matrix3x4 id = Identity3x4();
+      s.offset.insert(s.offset.end(), id.begin(), id.end());
+    }
     for (auto* v : {&s.inverse_mass, &s.linear_damping, &s.angular_damping, &s.motion, &s.radius}) v->assign(n, 0);
     s.is_awake.assign(n, 0);
     s.can_sleep.assign(n, 0);
@@ -407,22 +426,15 @@ struct Marshal {
 };
 
 namespace detail {
-inline bool identity(const Matrix3x4& m) { return m == Identity3x4(); }
-
 struct Shape {
   RigidBody* body;
   int shape;
   Vector3 half;
   Real radius;
+  Matrix3x4 offset;
 };
-inline Shape shape_of(const CollisionSphere& s) {
-  if (!identity(s.Offset)) throw Error(CZ_ERR_BAD_ARG, "CollisionSphere: only the identity Offset is supported");
-  return Shape{s.Body, CZ_SHAPE_SPHERE, Vector3{}, s.Radius};
-}
-inline Shape shape_of(const CollisionCube& c) {
-  if (!identity(c.Offset)) throw Error(CZ_ERR_BAD_ARG, "CollisionCube: only the identity Offset is supported");
-  return Shape{c.Body, CZ_SHAPE_CUBE, c.HalfSize, 0};
-}
+inline Shape shape_of(const CollisionSphere& s) { return Shape{s.Body, CZ_SHAPE_SPHERE, Vector3{}, s.Radius, s.Offset}; }
+inline Shape shape_of(const CollisionCube& c) { return Shape{c.Body, CZ_SHAPE_CUBE, c.HalfSize, 0, c.Offset}; }
 
 // Run one narrowphase test on the GPU and append its contacts: (a, b) is
 // CheckForCollisions(a, b); b == nullptr is a's CheckAgainstHalfSpace(plane).
@@ -432,8 +444,8 @@ inline bool collide(const Shape& a, const Shape* b, const CollisionPlane* plane,
   const int n = b ? 2 : 1;
   cz_batch* batch = rt.batch(n, 8);
   gpu::Staging s = Marshal::staging(n);
-  Marshal::put(s, 0, *a.body, a.shape, a.half, a.radius);
-  if (b) Marshal::put(s, 1, *b->body, b->shape, b->half, b->radius);
+  Marshal::put(s, 0, *a.body, a.shape, a.half, a.radius, a.offset);
+  if (b) Marshal::put(s, 1, *b->body, b->shape, b->half, b->radius, b->offset);
   cz_bodies v = s.view();
   check(cz_upload_bodies(batch, &v), "cz_upload_bodies");
   const int32_t unit[2] = {0, b ? 1 : -1};
@@ -489,6 +501,8 @@ inline bool CollisionPlane::CheckAgainstSphere(CollisionSphere& sphere, std::vec
 inline bool CollisionPlane::CheckAgainstCube(CollisionCube& cube, std::vector<Contact>& contacts) {
   return cube.CheckAgainstHalfSpace(*this, contacts);  // colliders.go:122-125
 }
+inline Matrix3x4 CollisionSphere::GetTransform() const { return MulMatrix3x4(Body->GetTransform(), Offset); }
+inline Matrix3x4 CollisionCube::GetTransform() const { return MulMatrix3x4(Body->GetTransform(), Offset); }
 inline bool CollisionSphere::CheckAgainstHalfSpace(const CollisionPlane& plane, std::vector<Contact>& contacts) {
   return detail::collide(detail::shape_of(*this), nullptr, &plane, contacts);
 }

@@ -90,6 +90,9 @@ typedef struct cz_bodies {
   double* radius;                  /* [n]     CollisionSphere.Radius */
   double* inverse_inertia_world;   /* [n][9]  derived; upload: NULL = CalculateDerivedData */
   double* last_frame_acceleration; /* [n][3]  derived; upload: NULL = zero */
+  double* collider_offset;         /* [n][12] CollisionCube/CollisionSphere.Offset (colliders.go:44,64), a
+                                    *          column-major Matrix3x4; upload: NULL = the identity that
+                                    *          NewCollisionCube/Sphere set (colliders.go:138,267) */
 } cz_bodies;
 
 /* One contact, the exported fields of Contact (contact.go:17-36).  Bodies are
@@ -125,7 +128,11 @@ int cz_step(cz_batch* batch, int32_t nsteps, double dt);
  * cz_step / cz_step_timed for nsteps without running them. */
 int cz_prepare_rollout(cz_batch* batch, int32_t nsteps, double dt);
 
-/* The three phases separately (blocking). */
+/* The three phases separately (blocking).  The narrowphase derives each
+ * collider's transform from its body's current position and orientation:
+ * what the reference's collider holds right after Integrate, the frame loop's
+ * order.  (After a resolve with no Integrate in between, the reference would
+ * still test the transforms of the last Integrate.) */
 int cz_integrate(cz_batch* batch, double dt);                   /* rigidbody.go:213-259 */
 int cz_narrowphase(cz_batch* batch);                            /* examples/cubedrop.go:41-67 */
 int cz_resolve(cz_batch* batch, double dt);                     /* contact.go:208-222 */

@@ -319,7 +319,7 @@ template <class A, class B> inline M3<A> cm3(const M3<B>& m) { M3<A> r; for (int
 enum Shape : int32_t { kSphere = 0, kCube = 1 };
 
 // RigidBody (rigidbody.go:23-101) merged with its collider (colliders.go:37-71);
-// the collider Offset is the identity set by NewCollisionSphere/Cube
+// the collider Offset defaults to the identity set by NewCollisionSphere/Cube
 // (colliders.go:138,267).  Orientation is kept in the island type W so the
 // precision form can accumulate adjustPositions corrections in FP64.
 template <class R, class W> struct Body {

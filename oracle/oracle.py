@@ -19,7 +19,8 @@ FP32 = 1
 class OrcBodies(C.Structure):
     _fields_ = [(name, C.c_void_p) for name in (
         "position", "orientation", "velocity", "rotation", "acceleration", "inverse_inertia", "inverse_mass",
-        "linear_damping", "angular_damping", "motion", "is_awake", "can_sleep", "shape", "half_size", "radius")]
+        "linear_damping", "angular_damping", "motion", "is_awake", "can_sleep", "shape", "half_size", "radius",
+        "collider_offset")]
 
 
 def lib():
@@ -33,6 +34,7 @@ def lib():
         L.orc_step.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_int, C.c_int]
         L.orc_integrate.argtypes = [C.c_void_p, C.c_double]
         L.orc_narrowphase.argtypes = [C.c_void_p]
+        L.orc_collide.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_int]
         L.orc_resolve.argtypes = [C.c_void_p, C.c_double, C.c_int]
         L.orc_get_bodies.argtypes = [C.c_void_p, C.POINTER(OrcBodies)]
         L.orc_contact_count.argtypes = [C.c_void_p, C.c_int]
@@ -87,6 +89,8 @@ class OracleBatch:
         self.form = form
         self._keep = {k: np.ascontiguousarray(getattr(scene, k), dtype=_DTYPES.get(k, np.float64))
                       for k in scene.FIELDS}
+        if getattr(scene, "collider_offset", None) is not None:
+            self._keep["collider_offset"] = np.ascontiguousarray(scene.collider_offset, dtype=np.float64)
         s = _bodies_struct(self._keep)
         self.h = self.L.orc_create(form, scene.num_worlds, _ptr(scene.counts), C.byref(s), _ptr(scene.plane))
 
@@ -103,6 +107,12 @@ class OracleBatch:
 
     def narrowphase(self):
         return self.L.orc_narrowphase(self.h)
+
+    def collide(self, world, units):
+        """The narrowphase tests of `units` ((i, j), j = -1 for the half-space)
+        of one world, in list order; replaces the world's contacts."""
+        u = np.ascontiguousarray(np.asarray(units, dtype=np.int32).reshape(-1, 2))
+        return self.L.orc_collide(self.h, int(world), _ptr(u), int(u.shape[0]))
 
     def resolve(self, dt=1.0 / 60.0, iter_mult=4):
         return self.L.orc_resolve(self.h, dt, iter_mult)

@@ -31,6 +31,7 @@ struct orc_bodies {
   int32_t* shape;           // [n] 0 sphere, 1 cube
   double* half_size;        // [n][3]
   double* radius;           // [n]
+  double* collider_offset;  // [n][12] collider Offset (column-major 3x4), null = identity
 };
 }
 
@@ -41,6 +42,7 @@ struct BatchBase {
   virtual uint32_t step(int nsteps, double dt, int iterMult, int nthreads) = 0;
   virtual void integrate(double dt) = 0;
   virtual uint32_t narrowphase() = 0;
+  virtual uint32_t collide(int w, const int32_t* units, int nunits) = 0;
   virtual uint32_t resolve(double dt, int iterMult) = 0;
   virtual void get(orc_bodies* out) = 0;
   virtual int contactCount(int w) = 0;
@@ -93,7 +95,11 @@ template <class R, class W> struct Batch : BatchBase {
       b.canSleep = in->can_sleep[i] != 0;
       b.shape = in->shape[i];
       b.radius = (R)in->radius[i];
-      SetIdentity(b.offset);
+      if (in->collider_offset) {
+        for (int k = 0; k < 12; ++k) b.offset[k] = (R)in->collider_offset[12 * i + k];
+      } else {
+        SetIdentity(b.offset);
+      }
       // Body.CalculateDerivedData + Collider.CalculateDerivedData at setup
       // (examples/cubedrop.go:171-172).
       CalculateDerivedData(b);
@@ -163,6 +169,25 @@ template <class R, class W> struct Batch : BatchBase {
       generated[w] = work[w];
       st[w].contacts = (int)work[w].size();
     }
+    return err;
+  }
+
+  // A caller's list of tests of world w in the caller's order: (i, -1) is
+  // body i's CheckAgainstHalfSpace(plane), (i, j) CheckForCollisions(i, j)
+  // (colliders.go:720-747); the world's contact list is replaced.
+  uint32_t collide(int w, const int32_t* units, int nunits) override {
+    uint32_t err = 0;
+    Body<R, W>* b = &bodies[start[w]];
+    work[w].clear();
+    for (int u = 0; u < nunits; ++u) {
+      const int i = units[2 * u], j = units[2 * u + 1];
+      if (j < 0)
+        CheckAgainstHalfSpace(b[i], i, plane, work[w]);
+      else
+        CheckForCollisions(b[i], i, b[j], j, work[w], err);
+    }
+    generated[w] = work[w];
+    st[w].contacts = (int)work[w].size();
     return err;
   }
 
@@ -288,6 +313,9 @@ int orc_step(void* h, int nsteps, double dt, int iterMult, int nthreads) {
 }
 void orc_integrate(void* h, double dt) { static_cast<BatchBase*>(h)->integrate(dt); }
 int orc_narrowphase(void* h) { return (int)static_cast<BatchBase*>(h)->narrowphase(); }
+int orc_collide(void* h, int w, const int32_t* units, int nunits) {
+  return (int)static_cast<BatchBase*>(h)->collide(w, units, nunits);
+}
 int orc_resolve(void* h, double dt, int iterMult) { return (int)static_cast<BatchBase*>(h)->resolve(dt, iterMult); }
 void orc_get_bodies(void* h, orc_bodies* out) { static_cast<BatchBase*>(h)->get(out); }
 int orc_contact_count(void* h, int w) { return static_cast<BatchBase*>(h)->contactCount(w); }
