@@ -111,7 +111,7 @@ class Scene:
         self.plane = np.ascontiguousarray(plane, dtype=np.float64)
         for name in self.FIELDS:
             setattr(self, name, arrays[name])
-        # [n, 12] collider Offsets (column-major 3x4, colliders.go:44,64); None = the identity
+        # [n, 12] collider Offsets (column-major 3x4, colliders.go:44,62); None = the identity
         self.collider_offset = arrays.get("collider_offset")
         self.name = arrays.get("name", "scene")
 
@@ -291,7 +291,7 @@ def _rotation_columns(q):
 
 def offsets(num_worlds=64, bodies=24, seed=9, nonrigid=0.125):
     """mixed()-type worlds of `bodies` bodies whose colliders carry an Offset
-    (CollisionCube/CollisionSphere.Offset, colliders.go:44,64): a uniform
+    (CollisionCube/CollisionSphere.Offset, colliders.go:44,62): a uniform
     rotation and a translation U[-0.3,0.3]^3.  A fraction `nonrigid` of the
     Offsets also scale their three axes by U[0.7,1.3] (the reference applies
     any 3x4 Offset; such a collider is not a rigid image of its box)."""

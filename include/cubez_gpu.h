@@ -90,7 +90,7 @@ typedef struct cz_bodies {
   double* radius;                  /* [n]     CollisionSphere.Radius */
   double* inverse_inertia_world;   /* [n][9]  derived; upload: NULL = CalculateDerivedData */
   double* last_frame_acceleration; /* [n][3]  derived; upload: NULL = zero */
-  double* collider_offset;         /* [n][12] CollisionCube/CollisionSphere.Offset (colliders.go:44,64), a
+  double* collider_offset;         /* [n][12] CollisionCube/CollisionSphere.Offset (colliders.go:44,62), a
                                     *          column-major Matrix3x4; upload: NULL = the identity that
                                     *          NewCollisionCube/Sphere set (colliders.go:138,267) */
 } cz_bodies;

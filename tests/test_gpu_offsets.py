@@ -1,4 +1,4 @@
-"""GPU parity, through the C ABI, for collider Offsets (colliders.go:44,64,
+"""GPU parity, through the C ABI, for collider Offsets (colliders.go:44,62,
 173-176, 302-304) and static infinite-mass bodies (the backboard of
 examples/ballistic.go:183-187): bit-identical to the oracle in both forms."""
 import numpy as np

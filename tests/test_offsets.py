@@ -1,6 +1,6 @@
 """Collider Offsets and static (infinite-mass) bodies on the oracle, CPU only.
 
-The reference's colliders carry an Offset (colliders.go:44,64) multiplied into
+The reference's colliders carry an Offset (colliders.go:44,62) multiplied into
 their transform (colliders.go:173-176, 302-304); its ballistic example keeps a
 backboard of infinite mass that it never integrates (examples/ballistic.go:
 183-187).  These tests pin the oracle's handling of both, which the GPU
