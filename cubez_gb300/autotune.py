@@ -4,6 +4,8 @@ Searches, on the caller's own batch and scene state, over
   * resolver lanes per world G (worlds per warp = 32 / G),
   * the resolver's shared-memory contact tile (contacts per world kept on chip),
   * the narrowphase CTA size,
+  * with worlds of more than 64 bodies in the batch, the large-world
+    resolver's lanes per world (32, or 16 = two worlds per warp),
   * with the learned warm start enabled, optionally the warm-start budget
     threshold (which worlds are warm-started; it changes which of two valid
     solutions a world gets, within the resolver's epsilon, and the speed),
@@ -17,13 +19,17 @@ search is reproducible; the snapshot should hold a representative
 """
 import itertools
 
+import numpy as np
+
 DEFAULT_LANES = (4, 8, 16, 32)
 DEFAULT_TILES = (64, 96, 128, 192)
 DEFAULT_NP_THREADS = (32, 64, 128, 256)
+DEFAULT_LARGE_LANES = (32, 16)
+BIG_WORLD = 64  # worlds of more bodies than this go to the large-world resolver
 
 
 def tune(batch, frames=30, dt=1.0 / 60.0, lanes=DEFAULT_LANES, tiles=DEFAULT_TILES, np_threads=DEFAULT_NP_THREADS,
-         warm_shifts=(), repeats=1, log=None):
+         warm_shifts=(), large_lanes=DEFAULT_LARGE_LANES, repeats=1, log=None):
     """Returns (best_config, trials); the batch is left at best_config."""
     trials = []
 
@@ -60,6 +66,15 @@ def tune(batch, frames=30, dt=1.0 / 60.0, lanes=DEFAULT_LANES, tiles=DEFAULT_TIL
         if best_ms is None or ph[2] < best_ms:
             best, best_ms = (g, cfg["resolver_contacts"]), ph[2]
     batch.set_tuning(resolver_lanes=best[0], resolver_contacts=best[1])
+    if large_lanes and (np.asarray(batch.counts) > BIG_WORLD).any():
+        best_ll, ll_ms = None, None
+        for g in large_lanes:
+            batch.set_tuning(large_world_lanes=g)
+            ph = measure()
+            trials.append({"large_world_lanes": g, "resolver_ms": float(ph[2])})
+            if ll_ms is None or ph[2] < ll_ms:
+                best_ll, ll_ms = g, ph[2]
+        batch.set_tuning(large_world_lanes=best_ll)
     if warm_shifts:
         best_shift, shift_ms = None, None
         for sh in warm_shifts:

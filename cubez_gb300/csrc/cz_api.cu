@@ -126,6 +126,7 @@ struct cz_batch {
   // tuning
   int np_threads = 128, np_grid = 1, rs_cs = 128, rs_grid = 1, rs_ctas_per_sm = 0, int_threads = 256;
   int rs_lanes = 8;  // lanes per world in the resolver (32 / rs_lanes worlds per warp)
+  int big_lanes = 32; // lanes per world in the large-world resolver (16: two worlds per warp)
   int mode = 0;      // resolver mode: 0 plain, 1 harvest, 2 learned warm start
   cz::MlpDev mlp{};  // device copy of the warm-start network
   void* mlp_mem = nullptr;
@@ -369,7 +370,7 @@ int launch_resolve_with(cz_batch* b, double dt, const cz::HostView& v, int cs, s
     }
   }
   if (!b->big_ids.empty()) {
-    CZ_CUDA(b->ops->resolve_big(v, (int)b->big_ids.size(), dt, b->stream));
+    CZ_CUDA(b->ops->resolve_big(v, (int)b->big_ids.size(), b->big_lanes, dt, b->stream));
     g_launches++;
   }
   return CZ_OK;
@@ -616,6 +617,11 @@ int cz_set_tuning(cz_batch* b, const cz_tuning* t) {
       return fail(CZ_ERR_BAD_ARG, "integrate_threads must be a multiple of 32, at most 256");
     b->int_threads = t->integrate_threads;
   }
+  if (t->large_world_lanes > 0) {
+    if (t->large_world_lanes != 16 && t->large_world_lanes != 32)
+      return fail(CZ_ERR_BAD_ARG, "large_world_lanes must be 16 or 32");
+    b->big_lanes = t->large_world_lanes;
+  }
   if (t->warm_start_budget_shift > 0) {
     if (t->warm_start_budget_shift > 8) return fail(CZ_ERR_BAD_ARG, "warm_start_budget_shift must be 1 to 8");
     b->warm_shift = t->warm_start_budget_shift;
@@ -631,6 +637,7 @@ int cz_get_tuning(cz_batch* b, cz_tuning* t) {
   t->integrate_threads = b->int_threads;
   t->resolver_lanes = b->rs_lanes;
   t->warm_start_budget_shift = b->warm_shift;
+  t->large_world_lanes = b->big_lanes;
   return CZ_OK;
 }
 

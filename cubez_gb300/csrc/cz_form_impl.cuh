@@ -301,9 +301,12 @@ static int warm_features_blocks(int nbs) {
   return blocks > 0 ? blocks : 1;
 }
 
-static cudaError_t resolve_big(const HostView& h, int nbig, double dt, cudaStream_t s) {
+static cudaError_t resolve_big(const HostView& h, int nbig, int lanes, double dt, cudaStream_t s) {
   if (nbig <= 0) return cudaSuccess;
-  k_resolve_big<R, W><<<nbig, 32, 0, s>>>(view_of(h), (R)dt);
+  if (lanes == 16)
+    k_resolve_big<R, W, 16><<<(nbig + 1) / 2, 32, 0, s>>>(view_of(h), (R)dt);
+  else
+    k_resolve_big<R, W, 32><<<nbig, 32, 0, s>>>(view_of(h), (R)dt);
   return cudaGetLastError();
 }
 

@@ -86,7 +86,8 @@ struct FormOps {
   // the learned paths' features / predictions ahead of the resolver (k_warm_features)
   cudaError_t (*warm_features)(const HostView& v, int nbs, int grid, double dt, cudaStream_t s);
   int (*warm_features_blocks)(int nbs);  // resident CTAs per SM
-  cudaError_t (*resolve_big)(const HostView& v, int nbig, double dt, cudaStream_t s);
+  // worlds above the shared-memory slot; `lanes` per world: 32, or 16 (two worlds per warp)
+  cudaError_t (*resolve_big)(const HostView& v, int nbig, int lanes, double dt, cudaStream_t s);
   cudaError_t (*resolve)(const HostView& v, int nbs, int cs, int lanes, int grid, size_t smem, double dt,
                          cudaStream_t s);
   // `off` ([n][12] doubles, the collider Offsets) may be null; the upload

@@ -1,9 +1,10 @@
 // ResolveContacts (contact.go:204-445) for worlds whose bodies do not fit the
 // shared-memory slot of k_resolve (hundreds to thousands of bodies).
 //
-// One warp per world.  Body and contact working rows live in global memory
-// (L2-resident at these sizes); the argmax over the world's contacts is the
-// same lane-strided scan and first-maximum butterfly as k_resolve.  After
+// One warp per world, or one per two worlds (16 lanes each).  Body and
+// contact working rows live in global memory (L2-resident at these sizes).
+// The argmax over a world's contacts is a lane-strided scan (four interleaved
+// chains per lane) and the first-maximum butterfly of k_resolve.  After
 // prepareContacts every body gets the list of its contacts (counting sort by
 // body, in global memory), so the update after each resolved contact visits
 // only the contacts of the two resolved bodies instead of all C: the
@@ -17,13 +18,14 @@
 
 namespace cz {
 
-// Visit every contact of bodies d0 and d1 once (lists adj[off[b] .. end[b])).
-template <class R, class W, class F>
+// Visit every contact of bodies d0 and d1 once (lists adj[off[b] .. end[b]))
+// with the G lanes of a group.
+template <int G, class R, class W, class F>
 __device__ __forceinline__ void for_pair_contacts(const RCtx<R, W>& x, const int* __restrict__ adj, const int* off,
-                                                  const int* end, int d0, int d1, int lane, F f) {
+                                                  const int* end, int d0, int d1, int gl, F f) {
   const int o0 = off[d0], l0 = end[d0] - o0;
   const int o1 = d1 >= 0 ? off[d1] : 0, l1 = d1 >= 0 ? end[d1] - o1 : 0;
-  for (int e = lane; e < l0 + l1; e += 32) {
+  for (int e = gl; e < l0 + l1; e += G) {
     int k;
     if (e < l0) {
       k = adj[o0 + e];
@@ -36,17 +38,77 @@ __device__ __forceinline__ void for_pair_contacts(const RCtx<R, W>& x, const int
   }
 }
 
-template <class R, class W>
+// The lane's first maximum of key_of(row[k], 0.01) over its contacts k = gl,
+// gl + G, ...: four interleaved running maxima (four independent compare
+// chains instead of one), each keeping its first maximum, merged by key and
+// then the smaller index.  The result is what one in-order scan of the
+// lane's contacts finds.
+template <int G, class R, class W>
+__device__ __forceinline__ void lane_first_max(const RCtx<R, W>& x, int row, int C, int gl,
+                                               decltype(key_of((R)0, (R)0))& best, int& bidx) {
+  using K = decltype(key_of((R)0, (R)0));
+  K b[4];
+  int ix[4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    b[q] = 0;
+    ix[q] = 0x7fffffff;
+  }
+  int k = gl;
+  for (; k + 3 * G < C; k += 4 * G) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const K key = key_of(x.Cf(row, k + G * q), (R)0.01);
+      if (key > b[q]) {
+        b[q] = key;
+        ix[q] = k + G * q;
+      }
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < 3; ++q) {  // at most three contacts left
+    const int kq = k + G * q;
+    if (kq < C) {
+      const K key = key_of(x.Cf(row, kq), (R)0.01);
+      if (key > b[q]) {
+        b[q] = key;
+        ix[q] = kq;
+      }
+    }
+  }
+#pragma unroll
+  for (int q = 1; q < 4; ++q) {
+    if (b[q] > b[0] || (b[q] == b[0] && ix[q] < ix[0])) {
+      b[0] = b[q];
+      ix[0] = ix[q];
+    }
+  }
+  best = b[0];
+  bidx = ix[0];
+}
+
+// One warp, 32 / G worlds of the large-world list (world blockIdx.x * 32 / G
+// + group), G lanes each.  With G = 16 the two worlds of a warp run their
+// iterations in lockstep, so the sequential part of each iteration (the
+// leader's float64 island arithmetic) is issued once for both.  Control flow
+// is uniform across the warp: a group whose world is missing or finished
+// keeps taking part in the warp-wide shuffles and barriers with its `run`
+// flag cleared.
+template <class R, class W, int G>
 __global__ void __launch_bounds__(32) k_resolve_big(BatchView<R> v, R dt) {
-  __shared__ R bc[16];
+  constexpr int NG = 32 / G;
+  __shared__ R bcs[NG][16];
   const int lane = threadIdx.x;
-  const int w = v.big_list[blockIdx.x];
-  const int n = v.body_count[w];
-  const int bstart = v.body_start[w];
-  const long long cst = v.contact_start[w];
+  const int grp = lane / G, gl = lane % G;
+  const int wi = blockIdx.x * NG + grp;
+  const bool has = wi < v.big_count;
+  const int w = has ? v.big_list[wi] : 0;
+  const int n = has ? v.body_count[w] : 0;
+  const int bstart = has ? v.body_start[w] : 0;
+  const long long cst = has ? v.contact_start[w] : 0;
   const long long S = v.nb_pad;
-  int C = v.contact_count[w];
-  const int cap = v.contact_cap[w];
+  int C = has ? v.contact_count[w] : 0;
+  const int cap = has ? v.contact_cap[w] : 0;
   if (C > cap) C = cap;  // the world is already flagged ST_CAPACITY
   RCtx<R, W> x;
   x.nbs = (int)S;  // row stride of the global body rows
@@ -54,7 +116,7 @@ __global__ void __launch_bounds__(32) k_resolve_big(BatchView<R> v, R dt) {
   x.bw = reinterpret_cast<W*>(v.big_bw) + bstart;
   x.br = v.big_br + bstart;
   x.aw = v.big_aw + bstart;
-  x.bc = bc;
+  x.bc = bcs[grp];
   x.cw = v.work + cst;
   x.cb = v.work_bodies + cst;
   x.cst = v.nc_total;
@@ -66,16 +128,15 @@ __global__ void __launch_bounds__(32) k_resolve_big(BatchView<R> v, R dt) {
   x.kw = reinterpret_cast<W*>(v.kmat) + cst;
   x.kr = v.kdv + cst;
   x.kst = v.nc_total;
-  const bool active = C > 0 && dt > (R)0;  // ResolveContacts guards, contact.go:210-212
-  if (!active) {
-    if (lane == 0) {
-      v.pos_iters[w] = 0;
-      v.vel_iters[w] = 0;
-      atomicAdd(&v.counters[3], (unsigned long long)C);
-    }
-    return;  // the whole block (one warp) leaves together
+  const bool active = has && C > 0 && dt > (R)0;  // ResolveContacts guards, contact.go:210-212
+  if (has && !active && gl == 0) {
+    v.pos_iters[w] = 0;
+    v.vel_iters[w] = 0;
+    atomicAdd(&v.counters[3], (unsigned long long)C);
   }
-  for (int i = lane; i < n; i += 32) {
+  const int na = active ? n : 0;
+  const int Ca = active ? C : 0;
+  for (int i = gl; i < na; i += G) {
     const long long g = bstart + i;
     x.P(0, i) = (W)v.body[B_PX * S + g];
     x.P(1, i) = (W)v.body[B_PY * S + g];
@@ -97,96 +158,91 @@ __global__ void __launch_bounds__(32) k_resolve_big(BatchView<R> v, R dt) {
     x.aw[i] = v.awake[g];
   }
   __syncwarp();
-  for (int k = lane; k < C; k += 32) prepare_contact(x, v, cst + k, k);
+  for (int k = gl; k < Ca; k += G) prepare_contact(x, v, cst + k, k);
   __syncwarp();
   // contact lists per body: count, exclusive scan, fill
   int* off = v.big_off + bstart;
   int* end = v.big_cnt + bstart;  // counts, then the fill cursor, then the list ends
   int* adj = v.big_adj + 2 * cst;
-  for (int i = lane; i < n; i += 32) end[i] = 0;
+  for (int i = gl; i < na; i += G) end[i] = 0;
   __syncwarp();
-  for (int k = lane; k < C; k += 32) {
+  for (int k = gl; k < Ca; k += G) {
     const int bb = x.cb[k];
     atomicAdd(&end[body0_of(bb)], 1);
     if (body1_of(bb) >= 0) atomicAdd(&end[body1_of(bb)], 1);
   }
   __syncwarp();
+  const int nmax = __reduce_max_sync(FULL, (unsigned)na);  // the scan's shuffles need every lane
   int carry = 0;
-  for (int base = 0; base < n; base += 32) {
-    const int i = base + lane;
-    const int c = i < n ? end[i] : 0;
+  for (int base = 0; base < nmax; base += G) {
+    const int i = base + gl;
+    const int c = i < na ? end[i] : 0;
     int s = c;
 #pragma unroll
-    for (int d = 1; d < 32; d <<= 1) {
-      const int y = __shfl_up_sync(FULL, s, d);
-      if (lane >= d) s += y;
+    for (int d = 1; d < G; d <<= 1) {
+      const int y = __shfl_up_sync(FULL, s, d, G);
+      if (gl >= d) s += y;
     }
-    if (i < n) {
+    if (i < na) {
       off[i] = carry + s - c;
       end[i] = carry + s - c;
     }
-    carry += __shfl_sync(FULL, s, 31);
+    carry += __shfl_sync(FULL, s, G - 1, G);
   }
   __syncwarp();
-  for (int k = lane; k < C; k += 32) {
+  for (int k = gl; k < Ca; k += G) {
     const int bb = x.cb[k];
     adj[atomicAdd(&end[body0_of(bb)], 1)] = k;
     if (body1_of(bb) >= 0) adj[atomicAdd(&end[body1_of(bb)], 1)] = k;
   }
   __syncwarp();
-  const int max_it = v.max_iterations >= 0 ? v.max_iterations : C * v.iter_mult;
+  const int max_it = active ? (v.max_iterations >= 0 ? v.max_iterations : C * v.iter_mult) : 0;
   // ---------------- adjustPositions, contact.go:231-283
   int pos_used = 0;
-  while (pos_used < max_it) {
+  bool run = active && max_it > 0;
+  while (__any_sync(FULL, run)) {
     auto best = key_of((R)0, (R)0);
     int bidx = 0x7fffffff;
-    for (int k = lane; k < C; k += 32) {
-      const auto key = key_of(x.Cf(W_PEN, k), (R)0.01);
-      if (key > best) {
-        best = key;
-        bidx = k;
-      }
+    if (run) lane_first_max<G>(x, W_PEN, C, gl, best, bidx);
+    group_first_max<G>(best, bidx);
+    if (best == 0) run = false;
+    if (run && gl == 0) match_awake(x, x.cb[bidx]);
+    __syncwarp();
+    apply_position_change<R, W, G>(x, v, bstart, bidx, run, gl);
+    __syncwarp();
+    if (run) {
+      const int rb = x.cb[bidx];
+      const int d0 = body0_of(rb), d1 = body1_of(rb);
+      for_pair_contacts<G>(x, adj, off, end, d0, d1, gl, [&](int k) { penetration_update(x, k, d0, d1); });
     }
-    group_first_max<32>(best, bidx);
-    if (best == 0) break;
-    if (lane == 0) match_awake(x, x.cb[bidx]);
     __syncwarp();
-    apply_position_change<R, W, 32>(x, v, bstart, bidx, true, lane);
-    __syncwarp();
-    const int rb = x.cb[bidx];
-    const int d0 = body0_of(rb), d1 = body1_of(rb);
-    for_pair_contacts(x, adj, off, end, d0, d1, lane, [&](int k) { penetration_update(x, k, d0, d1); });
-    __syncwarp();
-    ++pos_used;
+    if (run && ++pos_used >= max_it) run = false;
   }
-  for (int k = lane; k < C; k += 32) friction_prepare(x, k);
+  for (int k = gl; k < Ca; k += G) friction_prepare(x, k);
   __syncwarp();
   // ---------------- adjustVelocities, contact.go:388-445
   int vel_used = 0;
-  while (vel_used < max_it) {
+  run = active && max_it > 0;
+  while (__any_sync(FULL, run)) {
     auto best = key_of((R)0, (R)0);
     int bidx = 0x7fffffff;
-    for (int k = lane; k < C; k += 32) {
-      const auto key = key_of(x.Cf(W_DDV, k), (R)0.01);
-      if (key > best) {
-        best = key;
-        bidx = k;
-      }
-    }
-    group_first_max<32>(best, bidx);
-    if (best == 0) break;
-    if (lane == 0) {
+    if (run) lane_first_max<G>(x, W_DDV, C, gl, best, bidx);
+    group_first_max<G>(best, bidx);
+    if (best == 0) run = false;
+    if (run && gl == 0) {
       match_awake(x, x.cb[bidx]);
       apply_velocity_change<R, W, false>(x, v, w, bidx);
     }
     __syncwarp();
-    const int rb = x.cb[bidx];
-    const int d0 = body0_of(rb), d1 = body1_of(rb);
-    for_pair_contacts(x, adj, off, end, d0, d1, lane, [&](int k) { velocity_update(x, k, d0, d1); });
+    if (run) {
+      const int rb = x.cb[bidx];
+      const int d0 = body0_of(rb), d1 = body1_of(rb);
+      for_pair_contacts<G>(x, adj, off, end, d0, d1, gl, [&](int k) { velocity_update(x, k, d0, d1); });
+    }
     __syncwarp();
-    ++vel_used;
+    if (run && ++vel_used >= max_it) run = false;
   }
-  if (lane == 0) {
+  if (active && gl == 0) {
     v.pos_iters[w] = pos_used;
     v.vel_iters[w] = vel_used;
     atomicAdd(&v.counters[1], (unsigned long long)pos_used);
@@ -195,7 +251,7 @@ __global__ void __launch_bounds__(32) k_resolve_big(BatchView<R> v, R dt) {
   }
   if (v.contact_writeback) {
     const long long CS = v.nc_total;
-    for (int k = lane; k < C; k += 32) {
+    for (int k = gl; k < Ca; k += G) {
       R* o = v.contact + cst + k;
       o[C_NX * CS] = x.Cf(W_NX, k);
       o[C_NY * CS] = x.Cf(W_NY, k);
@@ -204,7 +260,7 @@ __global__ void __launch_bounds__(32) k_resolve_big(BatchView<R> v, R dt) {
       v.contact_bodies[cst + k] = x.cb[k];
     }
   }
-  for (int i = lane; i < n; i += 32) {
+  for (int i = gl; i < na; i += G) {
     const long long g = bstart + i;
     v.body[B_PX * S + g] = (R)x.P(0, i);
     v.body[B_PY * S + g] = (R)x.P(1, i);

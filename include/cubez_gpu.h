@@ -268,6 +268,8 @@ typedef struct cz_tuning {
   int32_t warm_start_budget_shift; /* learned warm start: a world is warm-started when its last
                                       solve used at most max_iterations >> shift iterations
                                       (1 to 8; default 2) */
+  int32_t large_world_lanes;   /* lanes per world of more than 64 bodies: 32 (the default) or
+                                  16 (two worlds per warp in lockstep) */
 } cz_tuning;
 int cz_set_tuning(cz_batch* batch, const cz_tuning* tuning);
 int cz_get_tuning(cz_batch* batch, cz_tuning* tuning);

@@ -142,6 +142,8 @@ def test_bad_arguments_on_a_live_batch(cuda_lib):
     assert b.L.cz_set_tuning(b.h, C.byref(t)) == 1  # not a multiple of 32
     t = _lib.Tuning(0, 0, 0, 0, 6)
     assert b.L.cz_set_tuning(b.h, C.byref(t)) == 1  # lanes per world must be 4, 8, 16 or 32
+    t = _lib.Tuning(0, 0, 0, 0, 0, 0, 8)
+    assert b.L.cz_set_tuning(b.h, C.byref(t)) == 1  # large-world lanes must be 16 or 32
     bad = {"bodies": np.array([[0, 7]], np.int32), "point": np.zeros((1, 3)), "normal": np.array([[1.0, 0, 0]]),
            "penetration": np.array([0.1]), "friction": np.array([0.9]), "restitution": np.array([0.1])}
     arr = _cz_contacts(bad)

@@ -1,8 +1,9 @@
 """Worlds larger than the resolver's shared-memory slot (more than 64
 bodies) go through k_resolve_big: bodies and contacts in global memory,
-per-body contact lists for the per-iteration update.  Same bar as the small
-worlds: bit-identical with the oracle in both forms, alone and mixed with
-small worlds in one batch."""
+per-body contact lists for the per-iteration update, 32 lanes per world or
+16 (two worlds per warp in lockstep).  Same bar as the small worlds:
+bit-identical with the oracle in both forms, alone and mixed with small
+worlds in one batch."""
 import numpy as np
 import pytest
 
@@ -18,7 +19,7 @@ pytestmark = pytest.mark.gpu
 DT = 1.0 / 60.0
 
 
-def _run(scene, form, frames, settle=0):
+def _run(scene, form, frames, settle=0, lanes=32):
     from cubez_gb300.batch import WorldBatch
     ref = OracleBatch(scene, form=ORC_FP64 if form == 0 else ORC_FP32)
     if settle:
@@ -29,17 +30,21 @@ def _run(scene, form, frames, settle=0):
             setattr(scene, k, st[k])
         ref = OracleBatch(scene, form=ORC_FP64 if form == 0 else ORC_FP32)
     gpu = WorldBatch.from_scene(scene, form=form)
+    gpu.set_tuning(large_world_lanes=lanes)
+    assert gpu.get_tuning()["large_world_lanes"] == lanes
     gpu.step(frames, DT)
     ref.step(frames, DT)
     return gpu, ref, scene
 
 
+@pytest.mark.parametrize("lanes", [16, 32])
 @pytest.mark.parametrize("form", [0, 1])
-def test_pile_worlds_bit_exact(form, cuda_lib):
-    # 80 cubes per world on a 5 x 4 x 4 lattice, dropped onto the plane
+def test_pile_worlds_bit_exact(form, lanes, cuda_lib):
+    # 80 cubes per world on a 5 x 4 x 4 lattice, dropped onto the plane; with
+    # 16 lanes the third world shares its warp with an empty group
     scene = scenes.piles(num_worlds=3, seed=51, nx=5, nz=4, ny=4)
     assert scene.counts.min() > 64
-    gpu, ref, _ = _run(scene, form, frames=45)
+    gpu, ref, _ = _run(scene, form, frames=45, lanes=lanes)
     g, r = gpu.download(), ref.bodies()
     assert_bodies_equal(g, r)
     gs, rs = gpu.stats(), ref.stats()
@@ -52,11 +57,12 @@ def test_pile_worlds_bit_exact(form, cuda_lib):
     assert_contacts_equal(gpu, ref, scene.num_worlds)
 
 
+@pytest.mark.parametrize("lanes", [16, 32])
 @pytest.mark.parametrize("form", [0, 1])
-def test_small_and_big_worlds_in_one_batch(form, cuda_lib):
+def test_small_and_big_worlds_in_one_batch(form, lanes, cuda_lib):
     scene = scenes.mixed(num_worlds=10, seed=52, min_bodies=30, max_bodies=110)
     assert (scene.counts > 64).any() and (scene.counts <= 64).any()
-    gpu, ref, _ = _run(scene, form, frames=20, settle=100)
+    gpu, ref, _ = _run(scene, form, frames=20, settle=100, lanes=lanes)
     assert_bodies_equal(gpu.download(), ref.bodies())
     gs, rs = gpu.stats(), ref.stats()
     assert rs["vel_iterations"].sum() > 100
