@@ -82,6 +82,31 @@ def tilted_cube_on_plane():
     return world([dict(shape="cube", pos=(0.0, 0.85, 0.0), half=(0.5, 0.5, 0.5), quat=q)])
 
 
+def cube_edge_down():
+    # turned 45 deg about z, one edge 0.01 under the plane: two vertex contacts
+    q = quat_axis(math.pi / 4, (0.0, 0.0, 1.0))
+    return world([dict(shape="cube", pos=(0.0, 0.5 * math.sqrt(2.0) - 0.01, 0.0), half=(0.5, 0.5, 0.5), quat=q)])
+
+
+def cube_below_plane():
+    # entirely under the plane: all eight vertices are contacts
+    return world([dict(shape="cube", pos=(0.0, -1.0, 0.0), half=(0.5, 0.5, 0.5))])
+
+
+def static_cube_singular_friction():
+    """A cube of infinite mass and zero inverse inertia moving down at 1 m/s,
+    0.005 into the plane: the friction solve's response matrix is zero, so
+    Invert returns the zero matrix (math/matrix.go:135-137), every impulse is
+    zero and adjustVelocities spends its whole budget on the same contact."""
+    sc = world([dict(shape="cube", pos=(0.0, 0.495, 0.0), half=(0.5, 0.5, 0.5), vel=(0.0, -1.0, 0.0))])
+    sc.inverse_mass[:] = 0.0
+    sc.inverse_inertia[:] = 0.0
+    sc.acceleration[:] = 0.0
+    return sc
+
+
 ALL = {"cube_resting": cube_resting, "sphere_resting": sphere_resting, "sphere_pair": sphere_pair,
        "cube_sphere": cube_sphere, "sphere_inside_cube": sphere_inside_cube, "cube_on_cube": cube_on_cube,
-       "cube_edge_edge": cube_edge_edge, "tilted_cube_on_plane": tilted_cube_on_plane}
+       "cube_edge_edge": cube_edge_edge, "tilted_cube_on_plane": tilted_cube_on_plane,
+       "cube_edge_down": cube_edge_down, "cube_below_plane": cube_below_plane,
+       "static_cube_singular_friction": static_cube_singular_friction}

@@ -101,6 +101,38 @@ def test_tilted_cube_single_vertex():
     np.testing.assert_allclose(c["penetration"][0], half_diag - 0.85, atol=1e-9)
 
 
+def test_cube_edge_down_two_vertex_contacts():
+    c = contacts_of(cases.cube_edge_down())
+    assert len(c["penetration"]) == 2
+    np.testing.assert_allclose(c["penetration"], 0.01, atol=1e-9)
+    np.testing.assert_allclose(c["point"][:, 0], 0.0, atol=1e-9)
+    assert sorted(np.round(c["point"][:, 2], 12).tolist()) == [-0.5, 0.5]
+
+
+def test_cube_below_plane_eight_vertex_contacts():
+    c = contacts_of(cases.cube_below_plane())
+    assert len(c["penetration"]) == 8
+    # penetration = offset - vertex distance (colliders.go:348-355): 0.5 or 1.5
+    assert sorted(c["penetration"].tolist()) == [0.5] * 4 + [1.5] * 4
+    assert np.all(c["bodies"] == [0, -1])
+
+
+@pytest.mark.parametrize("form", [0, 1])
+def test_singular_friction_solve_spends_the_budget(form):
+    sc = cases.static_cube_singular_friction()
+    ob = OracleBatch(sc, form=form)
+    ob.narrowphase()
+    assert len(ob.contacts(0)["penetration"]) == 4
+    ob.resolve(1.0 / 60.0, iter_mult=4)
+    st = ob.stats()
+    assert st["pos_iterations"][0] == 0            # 0.005 is under positionEpsilon
+    assert st["vel_iterations"][0] == 4 * 4        # the whole budget, len(contacts) * 4
+    b = ob.bodies()
+    assert np.array_equal(b["velocity"][0], [0.0, -1.0, 0.0])   # zero impulses
+    start = sc.position[0] if form == 0 else sc.position[0].astype(np.float32).astype(np.float64)
+    assert np.array_equal(b["position"][0], start)
+
+
 @pytest.mark.parametrize("name", sorted(cases.ALL))
 def test_cases_deterministic(name):
     a = contacts_of(cases.ALL[name]())
