@@ -599,7 +599,7 @@ __global__ void __launch_bounds__(256) k_narrowphase(BatchView<R> v, int nbs) {
   tl.shape = reinterpret_cast<int*>(tl.T + 12 * nbs);
   tl.cull = reinterpret_cast<float*>(tl.shape + nbs);
   int* scan = reinterpret_cast<int*>(tl.cull + 5 * nbs);  // [2][32] + [64] world id
-  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5, nwarps = (blockDim.x + 31) >> 5;
+  const int tid = threadIdx.x;
   if (tid == 0) mbar_init(bar, 1);
   __syncthreads();
   unsigned phase = 0;

@@ -63,7 +63,7 @@ constexpr Real kEpsilon = 1e-7;                               // m.Epsilon
 
 class Error : public std::runtime_error {
  public:
-  Error(int status, const std::string& what) : std::runtime_error(what), status(status) {}
+  Error(int code, const std::string& what) : std::runtime_error(what), status(code) {}
   int status;
 };
 
