@@ -8,7 +8,7 @@ from cubez_gb300 import scenes
 from oracle.oracle import FP32 as ORC_FP32
 from oracle.oracle import FP64 as ORC_FP64
 from oracle.oracle import OracleBatch
-from tests.test_gpu_parity import STATE, assert_bodies_equal, assert_contacts_equal
+from tests.test_gpu_parity import assert_bodies_equal, assert_contacts_equal
 
 pytestmark = pytest.mark.gpu
 
