@@ -5,7 +5,9 @@
 //   mirror_loops cubedrop|ballistic <in.bin> <out.bin> <frames>
 //
 // cubedrop  (examples/cubedrop.go:29-75): every body is integrated; for each
-//           body the half-space test, then every other body.
+//           body the half-space test, then every other body;
+//           ResolveContacts(len(contacts) * 4), the benchmark configurations'
+//           budget (the example itself passes 8).
 // ballistic (examples/ballistic.go:27-105): body 0 is the cube, body 1 the
 //           backboard (never integrated), bodies 2.. the bullets; the
 //           example's test order; ResolveContacts(len(contacts) * 8).
