@@ -54,6 +54,7 @@ def lib():
         L.orc_m3_mul.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
         L.orc_m3_invert.argtypes = [C.c_void_p, C.c_void_p]
         L.orc_m34_mul.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+        L.orc_set_as_transform.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
         L.orc_v3_op.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_double]
         L.orc_v3_dot.restype = C.c_double
         L.orc_v3_dot.argtypes = [C.c_void_p, C.c_void_p]

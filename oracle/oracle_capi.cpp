@@ -384,6 +384,12 @@ void orc_m34_mul(const double* a, const double* b, double* out) {
   M34<double> r = MulMatrix3x4(x, y);
   for (int i = 0; i < 12; ++i) out[i] = r[i];
 }
+// Matrix3x4.SetAsTransform, matrix.go:165-185
+void orc_set_as_transform(const double* pos, const double* q, double* out) {
+  M34<double> m;
+  SetAsTransform(m, mk3(pos[0], pos[1], pos[2]), Q4<double>{{q[0], q[1], q[2], q[3]}});
+  for (int i = 0; i < 12; ++i) out[i] = m[i];
+}
 // op: 0 Add, 1 AddScaled(s), 2 ComponentProduct, 3 Cross, 4 Sub, 5 MulWith(s), 6 Normalize
 void orc_v3_op(int op, double* v, const double* o, double s) {
   V3<double> a = mk3(v[0], v[1], v[2]), b = mk3(o[0], o[1], o[2]);
