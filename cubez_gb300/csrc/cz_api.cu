@@ -22,7 +22,7 @@
 #include "cz_layout.cuh"
 
 // Worlds of more bodies than this are resolved by k_resolve_big (bodies and
-// contacts in global memory, one warp per world).
+// contacts in global memory, 32 or 16 lanes per world).
 constexpr int kBigWorld = 64;
 
 namespace {
