@@ -15,11 +15,14 @@ Body setup follows the reference's own helpers:
   * SetMass stores 1/m (rigidbody.go:124-127); SetAwake(true) sets motion to
     2*sleepEpsilon (rigidbody.go:182-187).
 
-The five workloads:
+The workloads:
   cubedrop      1 world, 20 cubes (examples/cubedrop.go scene)
   mixed         many worlds of U{8..64} spheres/cubes
   precision     many worlds x 32 bodies, 16 spheres + 16 cubes
   piles         worlds x 1024 cubes on a 16x16x4 lattice
+  offsets       mixed-type worlds whose colliders carry Offsets
+  ballistic     examples/ballistic.go's scene: a cube, a static backboard and
+                bullets (its test order: ballistic_units)
 """
 import math
 
