@@ -84,3 +84,37 @@ def test_concat_with_empty_worlds():
     assert list(s.counts) == [0, 3, 0, 4] and s.num_bodies == 7
     np.testing.assert_array_equal(s.position[s.world_slice(3)], parts[1].position)
     assert s.world_slice(0) == slice(0, 0)
+
+
+def test_ballistic_setup_matches_the_example():
+    """examples/ballistic.go:149-231: cube mass 8 with the block inertia of
+    half size 1, bullets of mass 1.5 with 0.4 m r^2, a backboard of infinite
+    mass and zero inverse inertia, NewRigidBody's dampings."""
+    sc = scenes.ballistic(num_worlds=2, bullets=3, seed=5)
+    assert sc.counts.tolist() == [5, 5]
+    w0 = sc.world_slice(0)
+    inv_m = sc.inverse_mass[w0]
+    assert inv_m.tolist() == [1.0 / 8.0, 0.0, 1.0 / 1.5, 1.0 / 1.5, 1.0 / 1.5]
+    ii = sc.inverse_inertia[w0].reshape(-1, 3, 3)
+    assert np.array_equal(np.diag(ii[0]), np.full(3, 1.0 / (0.3 * 8.0 * 2.0)))
+    assert not ii[1].any()
+    assert np.array_equal(np.diag(ii[2]), np.full(3, 1.0 / (((0.4 * 1.5) * 0.2) * 0.2)))
+    assert sc.shape[w0].tolist() == [scenes.CUBE, scenes.CUBE] + [scenes.SPHERE] * 3
+    assert sc.can_sleep[w0].tolist() == [1, 0, 1, 1, 1]
+    assert not sc.acceleration[w0][1].any() and not sc.velocity[w0][1].any()
+    assert np.all(sc.velocity[w0][2:] == [0.0, 0.0, -40.0])
+    assert np.all(sc.linear_damping == 0.95) and np.all(sc.angular_damping == 0.95)
+
+
+def test_offsets_rigid_and_scaled():
+    sc = scenes.offsets(num_worlds=16, bodies=24, seed=6, nonrigid=0.25)
+    o = sc.collider_offset
+    assert o.shape == (sc.num_bodies, 12)
+    cols = o[:, :9].reshape(-1, 3, 3)
+    norms = np.linalg.norm(cols, axis=2)
+    rigid = np.all(np.abs(norms - 1.0) < 1e-12, axis=1)
+    assert 0 < (~rigid).sum() < len(rigid)
+    assert np.all((norms[~rigid] >= 0.7 - 1e-12) & (norms[~rigid] <= 1.3 + 1e-12))
+    assert np.all(np.abs(o[:, 9:]) <= 0.3)
+    again = scenes.offsets(num_worlds=16, bodies=24, seed=6, nonrigid=0.25)
+    assert np.array_equal(again.collider_offset, o)
