@@ -674,11 +674,19 @@ int cz_upload_bodies(cz_batch* b, const cz_bodies* in) {
   std::memcpy(b->h_stage_i32, in->shape, sizeof(int) * n);
   const bool has_off = in->collider_offset != nullptr;
   if (has_off && !b->d_offset) {
-    if (cudaMalloc(&b->d_offset, b->ops->real_size * 12 * std::max<long long>(b->nb_pad, 1)) != cudaSuccess ||
-        cudaMalloc((void**)&b->d_off_stage, sizeof(double) * 12 * n) != cudaSuccess ||
-        cudaMallocHost((void**)&b->h_off_stage, sizeof(double) * 12 * n) != cudaSuccess)
+    const size_t rows = b->ops->real_size * 12 * std::max<long long>(b->nb_pad, 1);
+    void* rows_d = nullptr;
+    double *stage_d = nullptr, *stage_h = nullptr;
+    if (cudaMalloc(&rows_d, rows) != cudaSuccess || cudaMalloc((void**)&stage_d, sizeof(double) * 12 * n) != cudaSuccess ||
+        cudaMallocHost((void**)&stage_h, sizeof(double) * 12 * n) != cudaSuccess) {
+      if (rows_d) cudaFree(rows_d);
+      if (stage_d) cudaFree(stage_d);
       return fail(CZ_ERR_CUDA, "cz_upload_bodies: Offset allocation failed");
-    CZ_CUDA(cudaMemsetAsync(b->d_offset, 0, b->ops->real_size * 12 * std::max<long long>(b->nb_pad, 1), b->stream));
+    }
+    b->d_offset = rows_d;
+    b->d_off_stage = stage_d;
+    b->h_off_stage = stage_h;
+    CZ_CUDA(cudaMemsetAsync(b->d_offset, 0, rows, b->stream));
   }
   if (has_off != b->has_offset) {
     drop_graphs(b);  // the narrowphase's view changes
