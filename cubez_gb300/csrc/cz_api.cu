@@ -274,13 +274,19 @@ void free_batch(cz_batch* b) {
     cudaGraphExecDestroy(kv.second.exec);
     for (cudaEvent_t e : kv.second.ev) cudaEventDestroy(e);
   }
-  void* dev[] = {b->d_offset, b->d_off_stage, b->ws_feat, b->d_units, b->d_big, b->big_bw, b->big_br, b->big_aw, b->big_off, b->big_cnt, b->big_adj, b->ws_rows, b->ws_int, b->ws_u8, b->ws_world, b->mlp_mem, b->hv_features, b->hv_labels, b->hv_count, b->snap_body, b->snap_u8, b->body, b->awake, b->can_sleep, b->shape, b->d_bstart, b->d_bcount, b->d_ccap, b->d_ccount,
-                 b->d_cstart, b->d_wstatus, b->d_piters, b->d_viters, b->contact, b->cbodies, b->work, b->wbodies, b->kmat, b->kdv,
-                 b->d_order, b->d_order_rs, b->d_queue, b->d_status, b->d_counters, b->d_h2p, b->d_stage, b->d_stage_u8, b->d_stage_i32,
-                 b->d_cstage, b->d_cstage_b, b->d_pow};
+  void* dev[] = {
+      b->d_offset,  b->d_off_stage, b->ws_feat,   b->d_units,     b->d_big,      b->big_bw,      b->big_br,
+      b->big_aw,    b->big_off,     b->big_cnt,   b->big_adj,     b->ws_rows,    b->ws_int,      b->ws_u8,
+      b->ws_world,  b->mlp_mem,     b->hv_features, b->hv_labels, b->hv_count,   b->snap_body,   b->snap_u8,
+      b->body,      b->awake,       b->can_sleep, b->shape,       b->d_bstart,   b->d_bcount,    b->d_ccap,
+      b->d_ccount,  b->d_cstart,    b->d_wstatus, b->d_piters,    b->d_viters,   b->contact,     b->cbodies,
+      b->work,      b->wbodies,     b->kmat,      b->kdv,         b->d_order,    b->d_order_rs,  b->d_queue,
+      b->d_status,  b->d_counters,  b->d_h2p,     b->d_stage,     b->d_stage_u8, b->d_stage_i32, b->d_cstage,
+      b->d_cstage_b, b->d_pow};
   for (void* p : dev)
     if (p) cudaFree(p);
-  void* host[] = {b->h_off_stage, b->h_stage, b->h_stage_u8, b->h_stage_i32, b->h_cstage, b->h_cstage_b, b->h_pow, b->h_status};
+  void* host[] = {b->h_off_stage, b->h_stage,    b->h_stage_u8, b->h_stage_i32,
+                  b->h_cstage,     b->h_cstage_b, b->h_pow,      b->h_status};
   for (void* p : host)
     if (p) cudaFreeHost(p);
   if (b->stream) cudaStreamDestroy(b->stream);
@@ -677,7 +683,8 @@ int cz_upload_bodies(cz_batch* b, const cz_bodies* in) {
     const size_t rows = b->ops->real_size * 12 * std::max<long long>(b->nb_pad, 1);
     void* rows_d = nullptr;
     double *stage_d = nullptr, *stage_h = nullptr;
-    if (cudaMalloc(&rows_d, rows) != cudaSuccess || cudaMalloc((void**)&stage_d, sizeof(double) * 12 * n) != cudaSuccess ||
+    if (cudaMalloc(&rows_d, rows) != cudaSuccess ||
+        cudaMalloc((void**)&stage_d, sizeof(double) * 12 * n) != cudaSuccess ||
         cudaMallocHost((void**)&stage_h, sizeof(double) * 12 * n) != cudaSuccess) {
       if (rows_d) cudaFree(rows_d);
       if (stage_d) cudaFree(stage_d);
@@ -831,14 +838,18 @@ static int get_timed(cz_batch* b, int nsteps, double dt, cz_batch::Timed** out) 
   for (auto& e : t.ev) CZ_CUDA(cudaEventCreate(&e));
   CZ_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
   const long long before = g_launches.load();
-  int cst = cudaEventRecordWithFlags(t.ev[0], b->stream, cudaEventRecordExternal) == cudaSuccess ? CZ_OK : CZ_ERR_CUDA;
+  auto record = [&](int k) {
+    return cudaEventRecordWithFlags(t.ev[k], b->stream, cudaEventRecordExternal) == cudaSuccess ? CZ_OK
+                                                                                                : CZ_ERR_CUDA;
+  };
+  int cst = record(0);
   for (int s = 0; s < nsteps && cst == CZ_OK; ++s) {
     cst = launch_integrate(b, dt);
-    if (!cst && cudaEventRecordWithFlags(t.ev[3 * s + 1], b->stream, cudaEventRecordExternal) != cudaSuccess) cst = CZ_ERR_CUDA;
+    if (!cst) cst = record(3 * s + 1);
     if (!cst) cst = launch_narrowphase(b);
-    if (!cst && cudaEventRecordWithFlags(t.ev[3 * s + 2], b->stream, cudaEventRecordExternal) != cudaSuccess) cst = CZ_ERR_CUDA;
+    if (!cst) cst = record(3 * s + 2);
     if (!cst) cst = launch_resolve(b, dt);
-    if (!cst && cudaEventRecordWithFlags(t.ev[3 * s + 3], b->stream, cudaEventRecordExternal) != cudaSuccess) cst = CZ_ERR_CUDA;
+    if (!cst) cst = record(3 * s + 3);
   }
   g_launches.store(before);
   cudaGraph_t graph = nullptr;
