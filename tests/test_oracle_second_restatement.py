@@ -1,0 +1,65 @@
+"""The C++ oracle's resolver against a second, independent restatement of
+contact.go in plain Python (oracle/contact_ref.py), bit for bit: the same
+frames' contact lists resolved by both, then every body's state, the
+iteration counts and the resolved contacts compared.  CPU only."""
+import numpy as np
+import pytest
+
+from cubez_gb300 import scenes
+from oracle import contact_ref
+from oracle.oracle import FP64, OracleBatch
+
+DT = 1.0 / 60.0
+
+
+def _python_world(o, sc, w, st):
+    sl = sc.world_slice(w)
+    bodies = []
+    for i in range(sl.start, sl.stop):
+        bodies.append({"position": st["position"][i].tolist(), "orientation": st["orientation"][i].tolist(),
+                       "velocity": st["velocity"][i].tolist(), "rotation": st["rotation"][i].tolist(),
+                       "iit": st["iit_world"][i].tolist(), "inverse_mass": float(sc.inverse_mass[i]),
+                       # right after Integrate with no forces: lastFrameAccelleration = Acceleration
+                       "lfa": sc.acceleration[i].tolist(), "awake": bool(st["is_awake"][i])})
+    c = o.contacts(w)
+    contacts = [contact_ref.Contact(int(b[0]) if b[0] >= 0 else None, int(b[1]) if b[1] >= 0 else None,
+                                    p.tolist(), n.tolist(), float(pen))
+                for b, p, n, pen in zip(c["bodies"], c["point"], c["normal"], c["penetration"])]
+    return bodies, contacts
+
+
+SCENES = {
+    "mixed_early": lambda: (scenes.mixed(num_worlds=8, seed=61, min_bodies=6, max_bodies=12), 40),
+    "mixed_landed": lambda: (scenes.mixed(num_worlds=8, seed=63, min_bodies=6, max_bodies=12), 150),
+    "mixed_crowded": lambda: (scenes.mixed(num_worlds=4, seed=64, min_bodies=20, max_bodies=24), 240),
+    # 3 x 3 x 2 cubes dropped into a pile: box-box contacts in both orders
+    "pile": lambda: (scenes.piles(num_worlds=3, seed=65, nx=3, nz=3, ny=2, spacing=1.1), 60),
+}
+
+
+@pytest.mark.parametrize("name", sorted(SCENES))
+def test_resolver_matches_second_restatement(name, oracle_lib):
+    sc, settle = SCENES[name]()
+    o = OracleBatch(sc, form=FP64)
+    o.step(settle, DT)
+    o.integrate(DT)
+    o.narrowphase()
+    st = o.bodies()
+    worlds = [_python_world(o, sc, w, st) for w in range(sc.num_worlds)]
+    o.resolve(DT, iter_mult=4)
+    after = o.bodies()
+    stats = o.stats()
+    resolved_any = 0
+    for w, (bodies, contacts) in enumerate(worlds):
+        pos_used, vel_used = contact_ref.resolve_contacts(len(contacts) * 4, contacts, bodies, DT)
+        assert (pos_used, vel_used) == (stats["pos_iterations"][w], stats["vel_iterations"][w]), w
+        resolved_any += vel_used
+        sl = sc.world_slice(w)
+        for k in ("position", "orientation", "velocity", "rotation"):
+            got = np.array([b[k] for b in bodies]).reshape(after[k][sl].shape)
+            assert np.array_equal(got, after[k][sl]), "world %d: %s differs" % (w, k)
+        rc = o.resolved_contacts(w)
+        assert np.array_equal(np.array([c.penetration for c in contacts]), rc["penetration"])
+        assert np.array_equal(np.array([c.normal for c in contacts]).reshape(-1, 3), rc["normal"])
+        assert [[c.bodies[0], -1 if c.bodies[1] is None else c.bodies[1]] for c in contacts] == rc["bodies"].tolist()
+    assert resolved_any > 0
