@@ -63,3 +63,47 @@ def test_resolver_matches_second_restatement(name, oracle_lib):
         assert np.array_equal(np.array([c.normal for c in contacts]).reshape(-1, 3), rc["normal"])
         assert [[c.bodies[0], -1 if c.bodies[1] is None else c.bodies[1]] for c in contacts] == rc["bodies"].tolist()
     assert resolved_any > 0
+
+
+NARROW_SCENES = {
+    "mixed": lambda: (scenes.mixed(num_worlds=6, seed=66, min_bodies=10, max_bodies=16), 120),
+    "pile": lambda: (scenes.piles(num_worlds=2, seed=67, nx=3, nz=3, ny=2, spacing=1.1), 60),
+    "offsets": lambda: (scenes.offsets(num_worlds=4, bodies=14, seed=68, nonrigid=0.3), 120),
+    "cubedrop": lambda: (scenes.cubedrop(seed=1), 150),
+    # 16 spheres + 16 cubes per world: box-sphere contacts in both orders
+    "precision": lambda: (scenes.precision(num_worlds=3, bodies=32, seed=69), 200),
+}
+
+
+@pytest.mark.parametrize("name", sorted(NARROW_SCENES))
+def test_narrowphase_matches_second_restatement(name, oracle_lib):
+    """The oracle's contact lists (every narrowphase branch the scenes reach,
+    in the reference's order) against oracle/colliders_ref.py."""
+    from oracle import colliders_ref
+    sc, settle = NARROW_SCENES[name]()
+    o = OracleBatch(sc, form=FP64)
+    o.step(settle, DT)
+    o.integrate(DT)
+    o.narrowphase()
+    st = o.bodies()
+    offs = sc.collider_offset if sc.collider_offset is not None else np.tile(scenes.IDENTITY_OFFSET,
+                                                                              (sc.num_bodies, 1))
+    kinds = set()
+    for w in range(sc.num_worlds):
+        sl = sc.world_slice(w)
+        bodies = [{"shape": int(sc.shape[i]), "half": sc.half_size[i].tolist(), "radius": float(sc.radius[i]),
+                   "position": st["position"][i].tolist(), "orientation": st["orientation"][i].tolist(),
+                   "velocity": st["velocity"][i].tolist(), "offset": offs[i].tolist()}
+                  for i in range(sl.start, sl.stop)]
+        got = colliders_ref.generate_contacts(bodies, sc.plane.tolist())
+        want = o.contacts(w)
+        assert len(got) == len(want["penetration"]), "world %d: %d vs %d contacts" % (w, len(got),
+                                                                                    len(want["penetration"]))
+        for k, (b0, b1, p, n, pen) in enumerate(got):
+            assert [b0, -1 if b1 is None else b1] == want["bodies"][k].tolist(), (w, k)
+            assert np.array_equal(p, want["point"][k]) and np.array_equal(n, want["normal"][k]), (w, k)
+            assert pen == want["penetration"][k], (w, k)
+            kinds.add((bodies[b0]["shape"], None if b1 is None else bodies[b1]["shape"]))
+    assert len(kinds) >= 2 and sum(len(o.contacts(w)["penetration"]) for w in range(sc.num_worlds)) > 0
+    if name == "precision":
+        assert (scenes.CUBE, scenes.SPHERE) in kinds
