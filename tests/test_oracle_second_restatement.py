@@ -107,3 +107,50 @@ def test_narrowphase_matches_second_restatement(name, oracle_lib):
     assert len(kinds) >= 2 and sum(len(o.contacts(w)["penetration"]) for w in range(sc.num_worlds)) > 0
     if name == "precision":
         assert (scenes.CUBE, scenes.SPHERE) in kinds
+
+
+def _frame_bodies(sc, w):
+    """The scene's bodies of world w as set up (CalculateDerivedData done)."""
+    from oracle import rigidbody_ref
+    sl = sc.world_slice(w)
+    offs = sc.collider_offset if sc.collider_offset is not None else np.tile(scenes.IDENTITY_OFFSET,
+                                                                              (sc.num_bodies, 1))
+    bodies = []
+    for i in range(sl.start, sl.stop):
+        b = {"shape": int(sc.shape[i]), "half": sc.half_size[i].tolist(), "radius": float(sc.radius[i]),
+             "position": sc.position[i].tolist(), "orientation": sc.orientation[i].tolist(),
+             "velocity": sc.velocity[i].tolist(), "rotation": sc.rotation[i].tolist(),
+             "acceleration": sc.acceleration[i].tolist(), "iit_body": sc.inverse_inertia[i].tolist(),
+             "inverse_mass": float(sc.inverse_mass[i]), "linear_damping": float(sc.linear_damping[i]),
+             "angular_damping": float(sc.angular_damping[i]), "can_sleep": bool(sc.can_sleep[i]),
+             "awake": bool(sc.is_awake[i]), "lfa": [0.0, 0.0, 0.0], "offset": offs[i].tolist()}
+        rigidbody_ref.calculate_derived_data(b)
+        bodies.append(b)
+    return bodies
+
+
+@pytest.mark.parametrize("name", ["cubedrop", "mixed", "offsets"])
+def test_frames_match_second_restatement(name, oracle_lib):
+    """Whole frames (Integrate, the ordered narrowphase, ResolveContacts) of
+    the Python restatement against the oracle's step, every frame."""
+    from oracle import rigidbody_ref
+    sc = {"cubedrop": lambda: scenes.cubedrop(seed=2),
+          "mixed": lambda: scenes.mixed(num_worlds=3, seed=70, min_bodies=8, max_bodies=12),
+          "offsets": lambda: scenes.offsets(num_worlds=2, bodies=10, seed=71, nonrigid=0.3)}[name]()
+    o = OracleBatch(sc, form=FP64)
+    worlds = [_frame_bodies(sc, w) for w in range(sc.num_worlds)]
+    total = 0
+    for fr in range(90):
+        o.step(1, DT)
+        st, stats = o.bodies(), o.stats()
+        for w, bodies in enumerate(worlds):
+            n, pit, vit = rigidbody_ref.step(bodies, sc.plane.tolist(), DT)
+            assert (n, pit, vit) == (stats["contacts"][w], stats["pos_iterations"][w],
+                                     stats["vel_iterations"][w]), (fr, w)
+            total += n
+            sl = sc.world_slice(w)
+            for k in ("position", "orientation", "velocity", "rotation"):
+                got = np.array([b[k] for b in bodies])
+                assert np.array_equal(got, st[k][sl]), "frame %d world %d: %s differs" % (fr, w, k)
+            assert np.array_equal(np.array([b["iit"] for b in bodies]), st["iit_world"][sl])
+    assert total > 50
