@@ -10,8 +10,8 @@ reference's float64 arithmetic; the test runs both restatements on the same
 contact sets and compares every bit.  Pure-Python loops: small worlds only.
 
 Vectors are lists of 3 floats, Matrix3 lists of 9 (column-major), Quat lists
-(w, x, y, z).  Bodies are dicts; every body must be awake (the sleep path is
-left to the C++ oracle's own tests).
+(w, x, y, z).  Bodies are dicts (see oracle/rigidbody_ref.py); a sleeping body
+needs its iit_body for the derived data that applyPositionChange refreshes.
 """
 import math
 
@@ -205,6 +205,15 @@ def _internals(c, bodies, dt):  # contact.go:59-85
     _desired(c, bodies, dt)
 
 
+def _match_awake_state(c, bodies):  # contact.go:185-202
+    if c.bodies[1] is None:
+        return
+    from oracle.rigidbody_ref import set_awake
+    a0, a1 = bodies[c.bodies[0]]["awake"], bodies[c.bodies[1]]["awake"]
+    if (a0 or a1) and not (a0 and a1):
+        set_awake(bodies[c.bodies[1]] if a0 else bodies[c.bodies[0]], True)
+
+
 def _apply_position_change(c, bodies, penetration):  # contact.go:286-386
     ang_i, lin_i = [0.0, 0.0], [0.0, 0.0]
     ang_m, lin_m = [0.0, 0.0], [0.0, 0.0]
@@ -250,6 +259,9 @@ def _apply_position_change(c, bodies, penetration):  # contact.go:286-386
         add_scaled(b["position"], c.normal, lin_m[i])
         quat_add_scaled_vector(b["orientation"], ang_change[i], 1.0)
         quat_normalize(b["orientation"])
+        if not b["awake"]:
+            from oracle.rigidbody_ref import calculate_derived_data
+            calculate_derived_data(b)
     return lin_change, ang_change
 
 
@@ -318,8 +330,6 @@ def resolve_contacts(max_iterations, contacts, bodies, dt):
     adjustPositions and adjustVelocities."""
     if dt <= 0.0 or not contacts:
         return 0, 0
-    if not all(b["awake"] for b in bodies):
-        raise NotImplementedError("sleeping bodies are not restated here")
     for c in contacts:  # prepareContacts, contact.go:225-229
         _internals(c, bodies, dt)
     pos_used = 0  # adjustPositions, contact.go:233-283
@@ -331,6 +341,7 @@ def resolve_contacts(max_iterations, contacts, bodies, dt):
         if index == len(contacts):
             break
         ct = contacts[index]
+        _match_awake_state(ct, bodies)
         lin, ang = _apply_position_change(ct, bodies, best)
         for c in contacts:
             for b in range(2):
@@ -352,6 +363,7 @@ def resolve_contacts(max_iterations, contacts, bodies, dt):
         if index == len(contacts):
             break
         ct = contacts[index]
+        _match_awake_state(ct, bodies)
         vel, rot = _apply_velocity_change(ct, bodies)
         for c in contacts:
             for b in range(2):

@@ -8,13 +8,14 @@ narrowphase of oracle/colliders_ref.py, ResolveContacts of
 oracle/contact_ref.py), written from the Go source independently of the C++
 oracle.  Bodies are the dicts of those two modules plus acceleration, iit_body
 (the body-space inverse inertia, column-major), linear_damping,
-angular_damping and can_sleep (must be false: the sleep path is left to the
-C++ oracle's own tests).
+angular_damping, can_sleep and motion.
 """
 import math
 
 from oracle import colliders_ref, contact_ref
-from oracle.contact_ref import add_scaled, m3_mul_vector, mul_with, quat_add_scaled_vector, quat_normalize
+from oracle.contact_ref import add_scaled, dot, m3_mul_vector, mul_with, quat_add_scaled_vector, quat_normalize
+
+SLEEP_EPSILON = 0.3  # rigidbody.go:14 (an untyped constant: 10 * it is exactly 3)
 
 
 def transform_inertia_tensor(iit_body, t):  # rigidbody.go:275-299
@@ -47,11 +48,19 @@ def calculate_derived_data(b):  # rigidbody.go:268-272
     b["iit"] = transform_inertia_tensor(b["iit_body"], t)
 
 
+def set_awake(b, awake):  # rigidbody.go:182-192
+    if awake:
+        b["awake"] = True
+        b["motion"] = SLEEP_EPSILON * 2.0
+    else:
+        b["awake"] = False
+        b["velocity"] = [0.0, 0.0, 0.0]
+        b["rotation"] = [0.0, 0.0, 0.0]
+
+
 def integrate(b, dt):  # rigidbody.go:213-259, no forces or torques accumulated
     if not b["awake"]:
         return
-    if b["can_sleep"]:
-        raise NotImplementedError("the sleep path is not restated here")
     force, torque = [0.0, 0.0, 0.0], [0.0, 0.0, 0.0]
     lfa = list(b["acceleration"])
     add_scaled(lfa, force, b["inverse_mass"])
@@ -64,6 +73,14 @@ def integrate(b, dt):  # rigidbody.go:213-259, no forces or torques accumulated
     add_scaled(b["position"], b["velocity"], dt)
     quat_add_scaled_vector(b["orientation"], b["rotation"], dt)
     calculate_derived_data(b)
+    if b["can_sleep"]:
+        current = dot(b["velocity"], b["velocity"]) + dot(b["rotation"], b["rotation"])
+        bias = math.pow(0.5, dt)
+        b["motion"] = bias * b["motion"] + (1.0 - bias) * current
+        if b["motion"] < SLEEP_EPSILON:
+            set_awake(b, False)
+        elif b["motion"] > 10 * SLEEP_EPSILON:
+            b["motion"] = 3.0
 
 
 def step(bodies, plane, dt, iter_mult=4):

@@ -123,24 +123,52 @@ def _frame_bodies(sc, w):
              "acceleration": sc.acceleration[i].tolist(), "iit_body": sc.inverse_inertia[i].tolist(),
              "inverse_mass": float(sc.inverse_mass[i]), "linear_damping": float(sc.linear_damping[i]),
              "angular_damping": float(sc.angular_damping[i]), "can_sleep": bool(sc.can_sleep[i]),
-             "awake": bool(sc.is_awake[i]), "lfa": [0.0, 0.0, 0.0], "offset": offs[i].tolist()}
+             "awake": bool(sc.is_awake[i]), "lfa": [0.0, 0.0, 0.0], "offset": offs[i].tolist(),
+             "motion": float(sc.motion[i])}
         rigidbody_ref.calculate_derived_data(b)
         bodies.append(b)
     return bodies
 
 
-@pytest.mark.parametrize("name", ["cubedrop", "mixed", "offsets"])
-def test_frames_match_second_restatement(name, oracle_lib):
+def _sleepy(make):
+    def f():
+        sc = make()
+        sc.can_sleep[:] = 1
+        return sc
+    return f
+
+
+FRAME_SCENES = {
+    "cubedrop": (lambda: scenes.cubedrop(seed=2), 90),
+    "mixed": (lambda: scenes.mixed(num_worlds=3, seed=70, min_bodies=8, max_bodies=12), 90),
+    "offsets": (lambda: scenes.offsets(num_worlds=2, bodies=10, seed=71, nonrigid=0.3), 90),
+    # CanSleep on: the motion average and SetAwake (13 of 28 bodies asleep at
+    # once), and in a pile matchAwakeState waking sleeping bodies (49 times)
+    "sleeping": (_sleepy(lambda: scenes.mixed(num_worlds=2, seed=74, min_bodies=12, max_bodies=14)), 400),
+    "sleeping_pile": (_sleepy(lambda: scenes.piles(num_worlds=1, seed=73, nx=3, nz=3, ny=2, spacing=1.1)), 300),
+}
+
+
+@pytest.mark.parametrize("name", sorted(FRAME_SCENES))
+def test_frames_match_second_restatement(name, oracle_lib, monkeypatch):
     """Whole frames (Integrate, the ordered narrowphase, ResolveContacts) of
     the Python restatement against the oracle's step, every frame."""
     from oracle import rigidbody_ref
-    sc = {"cubedrop": lambda: scenes.cubedrop(seed=2),
-          "mixed": lambda: scenes.mixed(num_worlds=3, seed=70, min_bodies=8, max_bodies=12),
-          "offsets": lambda: scenes.offsets(num_worlds=2, bodies=10, seed=71, nonrigid=0.3)}[name]()
+    transitions = {"sleep": 0, "wake": 0}
+    set_awake = rigidbody_ref.set_awake
+
+    def counting_set_awake(b, awake):
+        if awake != b["awake"]:
+            transitions["wake" if awake else "sleep"] += 1
+        set_awake(b, awake)
+
+    monkeypatch.setattr(rigidbody_ref, "set_awake", counting_set_awake)
+    make, frames = FRAME_SCENES[name]
+    sc = make()
     o = OracleBatch(sc, form=FP64)
     worlds = [_frame_bodies(sc, w) for w in range(sc.num_worlds)]
     total = 0
-    for fr in range(90):
+    for fr in range(frames):
         o.step(1, DT)
         st, stats = o.bodies(), o.stats()
         for w, bodies in enumerate(worlds):
@@ -153,4 +181,10 @@ def test_frames_match_second_restatement(name, oracle_lib):
                 got = np.array([b[k] for b in bodies])
                 assert np.array_equal(got, st[k][sl]), "frame %d world %d: %s differs" % (fr, w, k)
             assert np.array_equal(np.array([b["iit"] for b in bodies]), st["iit_world"][sl])
+            assert np.array_equal(np.array([b["motion"] for b in bodies]), st["motion"][sl])
+            assert [int(b["awake"]) for b in bodies] == st["is_awake"][sl].tolist()
     assert total > 50
+    if name == "sleeping":
+        assert transitions["sleep"] > 10
+    if name == "sleeping_pile":
+        assert transitions["wake"] > 10  # matchAwakeState woke sleeping bodies
