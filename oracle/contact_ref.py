@@ -299,13 +299,30 @@ def _friction_impulse(c, bodies, iits):  # contact.go:535-606
     return ic
 
 
+class NilBody(Exception):
+    """calculateFrictionlessImpulse on a single-body contact: the reference's
+    inverted nil test (contact.go:512) dereferences the missing body."""
+
+
+def _frictionless_impulse(c, bodies, iits):  # contact.go:496-531
+    d = cross(c.rel[0], c.normal)
+    d = m3_mul_vector(iits[0], d)
+    d = cross(d, c.rel[0])
+    dv = dot(d, c.normal)
+    dv += bodies[c.bodies[0]]["inverse_mass"]
+    if c.bodies[1] is None:  # sic: the second body is added only when there is none
+        raise NilBody()
+    return [c.desired / dv, 0.0, 0.0]
+
+
 def _apply_velocity_change(c, bodies):  # contact.go:447-494
     iits = [bodies[c.bodies[0]]["iit"], [0.0] * 9]
     if c.bodies[1] is not None:
         iits[1] = bodies[c.bodies[1]]["iit"]
     if c.friction == 0.0:
-        raise NotImplementedError("frictionless contacts (contact.go:498-531) are not restated here")
-    ic = _friction_impulse(c, bodies, iits)
+        ic = _frictionless_impulse(c, bodies, iits)
+    else:
+        ic = _friction_impulse(c, bodies, iits)
     impulse = m3_mul_vector(c.to_world, ic)
     vel = [[0.0] * 3, [0.0] * 3]
     rot = [[0.0] * 3, [0.0] * 3]

@@ -188,3 +188,69 @@ def test_frames_match_second_restatement(name, oracle_lib, monkeypatch):
         assert transitions["sleep"] > 10
     if name == "sleeping_pile":
         assert transitions["wake"] > 10  # matchAwakeState woke sleeping bodies
+
+
+def test_resolver_materials_match_second_restatement(oracle_lib):
+    """Per-contact friction and restitution (the fields the resolver reads;
+    the colliders write 0.9 and 0.1): frictionless two-body contacts take
+    calculateFrictionlessImpulse with its inverted nil test (only the first
+    body's response), the others the friction solve with varied friction and
+    restitution."""
+    sc = scenes.mixed(num_worlds=6, seed=75, min_bodies=16, max_bodies=20)
+    o = OracleBatch(sc, form=FP64)
+    o.step(200, DT)
+    o.integrate(DT)
+    o.narrowphase()
+    st = o.bodies()
+    rng = np.random.default_rng(5)
+    worlds = []
+    for w in range(sc.num_worlds):
+        bodies, contacts = _python_world(o, sc, w, st)
+        c = o.contacts(w)
+        n = len(contacts)
+        two = c["bodies"][:, 1] >= 0
+        fric = np.where(two, 0.0, rng.uniform(0.2, 1.0, n))
+        rest = rng.uniform(0.0, 0.6, n)
+        for k, ct in enumerate(contacts):
+            ct.friction, ct.restitution = float(fric[k]), float(rest[k])
+        o.set_contacts(w, {"bodies": c["bodies"], "point": c["point"], "normal": c["normal"],
+                           "penetration": c["penetration"], "friction": fric, "restitution": rest})
+        worlds.append((bodies, contacts, int((fric == 0).sum())))
+    max_it = 200
+    o.resolve_fixed(max_it, DT)
+    after, stats = o.bodies(), o.stats()
+    frictionless = 0
+    for w, (bodies, contacts, nf) in enumerate(worlds):
+        pit, vit = contact_ref.resolve_contacts(max_it, contacts, bodies, DT)
+        assert (pit, vit) == (stats["pos_iterations"][w], stats["vel_iterations"][w]), w
+        sl = sc.world_slice(w)
+        for k in ("position", "orientation", "velocity", "rotation"):
+            got = np.array([b[k] for b in bodies]).reshape(after[k][sl].shape)
+            assert np.array_equal(got, after[k][sl]), "world %d: %s differs" % (w, k)
+        frictionless += nf
+    assert frictionless > 5
+
+
+def test_frictionless_single_body_contact_is_the_nil_case(oracle_lib):
+    """A frictionless contact with one body reaches the reference's nil
+    dereference (contact.go:512): the Python restatement raises, the oracle
+    reports it as a status bit (the C ABI's CZ_ERR_FRICTIONLESS)."""
+    sc = scenes.cubedrop(seed=1)
+    o = OracleBatch(sc, form=FP64)
+    o.step(30, DT)
+    o.integrate(DT)
+    o.narrowphase()
+    st = o.bodies()
+    bodies, contacts = _python_world(o, sc, 0, st)
+    c = o.contacts(0)
+    one = c["bodies"][:, 1] < 0
+    assert one.any()
+    fric = np.where(one, 0.0, 0.9)
+    for k, ct in enumerate(contacts):
+        ct.friction = float(fric[k])
+    o.set_contacts(0, {"bodies": c["bodies"], "point": c["point"], "normal": c["normal"],
+                       "penetration": c["penetration"], "friction": fric, "restitution": np.full(len(fric), 0.1)})
+    status = o.resolve_fixed(4 * len(fric), DT)
+    assert status & 2  # the frictionless-nil bit
+    with pytest.raises(contact_ref.NilBody):
+        contact_ref.resolve_contacts(4 * len(fric), contacts, bodies, DT)
