@@ -7,7 +7,8 @@ library's scratch is its statically reserved array.
 Checked against the allocating entry point cz_resolve_contacts on the same
 inputs, bit for bit (the tolerance of every parity test in this suite), on two
 calls in a row so that the second call starts from the scratch contents the
-first one left behind."""
+first one left behind.  Last, both entry points with per-contact friction and
+restitution against the oracle."""
 import ctypes as C
 
 import numpy as np
@@ -126,3 +127,47 @@ def test_static_scratch_rejects_sizes_beyond_its_maximum(cuda_lib):
     s = _lib.Bodies()
     assert cuda_lib.cz_resolve_contacts_static(0, 4, None, 1, DT, C.byref(s), 65, None) == 1
     assert cuda_lib.cz_resolve_contacts_static(0, 4, None, 8193, DT, C.byref(s), 8, None) == 1
+
+
+@pytest.mark.parametrize("form", [0, 1])
+def test_resolve_contacts_with_contact_materials(form, cuda_lib):
+    """Per-contact friction and restitution, the exported Contact fields the
+    resolver reads (the colliders write 0.9 and 0.1): every two-body contact
+    frictionless (calculateFrictionlessImpulse, contact.go:496-531, with its
+    inverted nil test), the single-body ones with friction in [0.2, 1], and
+    restitution in [0, 0.6].  The allocating entry point against the oracle,
+    and the allocation-free one against it, bit for bit."""
+    from oracle.oracle import OracleBatch
+    from tests.test_gpu_api import _resolve_both
+    # a 3 x 3 x 2 pile one second after the drop: 50 contacts, 24 between cubes
+    scene = scenes.piles(num_worlds=1, seed=76, nx=3, nz=3, ny=2, spacing=1.1)
+    ref = OracleBatch(scene)
+    ref.step(60, DT)
+    st = ref.bodies()
+    scene = scene.copy()
+    for k in ("position", "orientation", "velocity", "rotation"):
+        setattr(scene, k, st[k])
+    ref = OracleBatch(scene)
+    ref.narrowphase()
+    c = ref.contacts(0)
+    n = len(c["penetration"])
+    rng = np.random.default_rng(9)
+    two = c["bodies"][:, 1] >= 0
+    c["friction"] = np.where(two, 0.0, rng.uniform(0.2, 1.0, n))
+    c["restitution"] = rng.uniform(0.0, 0.6, n)
+    assert two.sum() > 10 and (~two).sum() > 10
+    st, arrays, arr, ref, _ = _resolve_both(scene, c, 4 * n, form)
+    assert st == 0, cuda_lib.cz_last_error()
+    assert ref.stats()["vel_iterations"][0] > 20
+    r = ref.bodies()
+    for k in ("position", "orientation", "velocity", "rotation"):
+        np.testing.assert_array_equal(arrays[k], r[k], err_msg=k)
+    rc = ref.resolved_contacts(0)
+    np.testing.assert_array_equal(np.array([arr[i].penetration for i in range(n)]), rc["penetration"])
+    # the allocation-free entry point on the same materials
+    from tests.test_gpu_api import _cz_contacts
+    arr_s = _cz_contacts(c)
+    st_s, out, out_contacts = _with_static_entry_point(cuda_lib, scene, arr_s, form)
+    assert st_s == 0, cuda_lib.cz_last_error()
+    for k in ("position", "orientation", "velocity", "rotation"):
+        np.testing.assert_array_equal(out[k], arrays[k], err_msg=k)
