@@ -33,7 +33,9 @@ learned warm start serves worlds within the resolver's shared-memory slot
 only, so the large worlds run the plain precision form.
 
 --impl reference times the reference's CPU path (the oracle port; the Go
-reference cannot be built here) on all host cores with the same metric.
+reference cannot be built here) on all host cores with the same metric; with
+--workload piles, the ordered narrowphase of one pile world per host thread,
+in pair-tests/s.
 """
 import argparse
 import json
@@ -398,9 +400,51 @@ def cpu_baseline(args, scene):
             "sample": "%d of %d worlds x %d frames (float64 oracle, %.1f s)" % (nw, scene.num_worlds, args.frames, el)}
 
 
+def run_reference_piles(args):
+    """The large-world metric (narrowphase pair-tests/s) on the oracle: the
+    ordered all-pairs narrowphase of a sample of pile worlds, one world per
+    host thread (each world its own oracle batch; the calls release the GIL)."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    from cubez_gb300 import scenes
+    from oracle.oracle import OracleBatch, hardware_threads
+    cores = os.cpu_count() or hardware_threads()
+    nw = args.worlds if args.worlds != 16384 else 256
+    sample = min(nw, cores)
+    scene = scenes.piles(num_worlds=nw, seed=5)
+    n = int(scene.counts[0])
+    units = sample * (n * (n - 1) + n)
+    batches = [OracleBatch(scene.subset([w])) for w in range(sample)]
+    for ob in batches:
+        ob.integrate(DT)
+    total = 0.0
+    with ThreadPoolExecutor(cores) as ex:
+        for _ in range(args.warmup):
+            list(ex.map(lambda ob: ob.narrowphase(), batches))
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            list(ex.map(lambda ob: ob.narrowphase(), batches))
+            total += time.perf_counter() - t0
+    value = units * args.steps / total
+    line = {"metric": "pair-tests/s (large worlds, secondary)", "value": value, "unit": "pair-tests/s",
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": total / args.steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded scenes)", "impl": "reference",
+            "config": {"workload": "piles: %d worlds x %d cubes; each step the narrowphase of %d worlds" %
+                                   (nw, n, sample), "parallelism": "host cores, one thread per world"},
+            "cpu_baseline": {"value": value, "unit": "pair-tests/s", "cores": cores, "kind": "port",
+                             "sample": "%d of %d worlds, first frame (the Go reference cannot be built here; its "
+                                       "float64 path restated in C++)" % (sample, nw)},
+            "e2e": {"value": value, "unit": "pair-tests/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
 def run_reference(args):
     ws, rank, _ = _dist()
     if rank != 0:
+        return
+    if args.workload == "piles":
+        run_reference_piles(args)
         return
     from cubez_gb300 import scenes
     from oracle.oracle import OracleBatch, hardware_threads
