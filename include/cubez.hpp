@@ -526,6 +526,21 @@ inline bool CollisionCube::CheckAgainstCube(CollisionCube& cube, std::vector<Con
   return detail::collide(detail::shape_of(*this), &other, nullptr, contacts);
 }
 
+// The Go package's constructor functions, returning owned objects where Go
+// returns pointers (rigidbody.go:104-114, colliders.go:81-86, 136-141,
+// 265-270, contact.go:54-57).  A collider given no body owns a new one.
+inline std::unique_ptr<RigidBody> NewRigidBody() { return std::make_unique<RigidBody>(); }
+inline std::unique_ptr<CollisionPlane> NewCollisionPlane(const Vector3& n, Real o) {
+  return std::make_unique<CollisionPlane>(n, o);
+}
+inline std::unique_ptr<CollisionSphere> NewCollisionSphere(RigidBody* optBody, Real radius) {
+  return std::make_unique<CollisionSphere>(optBody, radius);
+}
+inline std::unique_ptr<CollisionCube> NewCollisionCube(RigidBody* optBody, const Vector3& halfSize) {
+  return std::make_unique<CollisionCube>(optBody, halfSize);
+}
+inline Contact NewContact() { return Contact{}; }
+
 // CheckForCollisions, colliders.go:720-747: dispatch on the second collider's type
 inline bool CheckForCollisions(Collider& one, Collider& two, std::vector<Contact>& contacts) {
   if (auto* s = dynamic_cast<CollisionSphere*>(&two)) return one.CheckAgainstSphere(*s, contacts);

@@ -1,6 +1,8 @@
 // The C++ mirror's host-side setup math (include/cubez.hpp: MulMatrix3x4,
 // Invert, BlockInertiaTensor, AsTransform, RealEqual), run on records read
-// from a file, for comparison with the oracle bit for bit.  Uses no GPU.
+// from a file, for comparison with the oracle bit for bit, after a check of
+// the Go constructor functions' defaults (exit 3 if one is wrong).  Uses no
+// GPU.
 //
 //   host_math <in.bin> <out.bin>
 //
@@ -16,8 +18,24 @@
 
 using namespace cubez;
 
+// The Go constructor functions give the Go defaults (rigidbody.go:104-114,
+// colliders.go:81-86, 136-141, 265-270, contact.go:54-57).
+static bool constructors_ok() {
+  auto body = NewRigidBody();
+  auto plane = NewCollisionPlane(Vector3{0, 1, 0}, 2.5);
+  auto cube = NewCollisionCube(nullptr, Vector3{0.5, 0.25, 1});
+  auto sphere = NewCollisionSphere(body.get(), 0.75);
+  const Contact c = NewContact();
+  return body->LinearDamping == 0.95 && body->AngularDamping == 0.95 && body->Acceleration[1] == -9.78 &&
+         body->Orientation == Quat{1, 0, 0, 0} && body->IsAwake && body->CanSleep && !body->HasFiniteMass() &&
+         plane->Offset == 2.5 && cube->GetBody() != nullptr && cube->Offset == Identity3x4() &&
+         sphere->GetBody() == body.get() && sphere->Radius == 0.75 && c.Bodies[0] == nullptr &&
+         c.Penetration == 0 && c.Friction == 0;
+}
+
 int main(int argc, char** argv) {
   if (argc != 3) return 2;
+  if (!constructors_ok()) return 3;
   std::FILE* f = std::fopen(argv[1], "rb");
   if (!f) return 2;
   std::vector<double> in;
