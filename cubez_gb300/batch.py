@@ -18,6 +18,10 @@ _WIDTH = {"position": 3, "orientation": 4, "velocity": 3, "rotation": 3, "accele
           "collider_offset": 12}
 
 
+# the collider Offset NewCollisionCube / NewCollisionSphere set (colliders.go:138, 267)
+_IDENTITY_OFFSET = np.array([1.0, 0.0, 0.0, 0.0, 1.0, 0.0, 0.0, 0.0, 1.0, 0.0, 0.0, 0.0])
+
+
 def _ptr(a):
     return None if a is None else a.ctypes.data_as(C.c_void_p)
 
@@ -39,6 +43,8 @@ class WorldBatch:
         self.num_worlds = int(self.counts.shape[0])
         self.num_bodies = int(self.counts.sum())
         self.form = form
+        self.desc = {"plane": [float(x) for x in plane], "contact_capacity": int(contact_capacity),
+                     "iteration_multiplier": int(iteration_multiplier), "max_iterations": int(max_iterations)}
         d = _lib.BatchDesc()
         d.form = form
         d.num_worlds = self.num_worlds
@@ -94,6 +100,29 @@ class WorldBatch:
         s = bodies_struct(out)
         check(self.L.cz_download_bodies(self.h, C.byref(s)))
         return out
+
+    # ---------------------------------------------------------------- checkpoint
+    def save(self, path):
+        """Write the batch's description and full body state (derived data,
+        motion, awake flags and collider Offsets included) to an .npz file."""
+        state = self.download(tuple(_WIDTH))
+        if np.array_equal(state["collider_offset"], np.tile(_IDENTITY_OFFSET, (self.num_bodies, 1))):
+            del state["collider_offset"]
+        np.savez(path, counts=self.counts, form=np.int32(self.form), plane=np.array(self.desc["plane"]),
+                 contact_capacity=np.int32(self.desc["contact_capacity"]),
+                 iteration_multiplier=np.int32(self.desc["iteration_multiplier"]),
+                 max_iterations=np.int32(self.desc["max_iterations"]), **state)
+
+    @classmethod
+    def load(cls, path, device=0):
+        """A new batch holding the state `save` wrote; it steps on exactly as
+        the saved batch would (tuning is not saved: it changes no result)."""
+        z = np.load(path)
+        b = cls(z["counts"], form=int(z["form"]), plane=z["plane"], contact_capacity=int(z["contact_capacity"]),
+                iteration_multiplier=int(z["iteration_multiplier"]), max_iterations=int(z["max_iterations"]),
+                device=device)
+        b.upload(**{k: z[k] for k in _WIDTH if k in z.files})
+        return b
 
     # ---------------------------------------------------------------- stepping
     def step(self, nsteps=1, dt=1.0 / 60.0):
