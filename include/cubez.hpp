@@ -29,7 +29,10 @@
  *    impulse, a box-box test reaching no axis), a cubez::Error carrying the
  *    cz_status is thrown;
  *  - a collider's transform (body transform x Offset) is derived where it is
- *    used, so CalculateDerivedData on a collider has nothing to store.
+ *    used, so CalculateDerivedData on a collider has nothing to store;
+ *  - the constructor functions (NewRigidBody, NewCollisionPlane/Sphere/Cube)
+ *    return std::unique_ptr where Go returns a pointer, and NewContact a
+ *    value.
  *
  * Host-side setup helpers (SetBlockInertiaTensor, Invert, SetAsTransform)
  * compute what the Go setup code computes once per body; they are not on the
