@@ -11,11 +11,12 @@ worlds only.
 A body is a dict with shape (0 sphere, 1 cube), half (3), radius, position
 (3), orientation (w, x, y, z), velocity (3) and offset (12, column-major,
 the collider's Offset).  A contact is (body0, body1 or None, point, normal,
-penetration).
+penetration).  With numpy float32 values (and a float32 plane) it states the
+precision form's narrowphase, which is float32 throughout.
 """
-import math
+import numpy as np
 
-from oracle.contact_ref import EPSILON, MAX_VALUE, cross, dot, magnitude, mul_with, real_equal
+from oracle.contact_ref import EPSILON, MAX_VALUE, cross, dot, magnitude, mul_with, real_equal, real_type, sqrt_
 
 SPHERE, CUBE = 0, 1
 
@@ -150,14 +151,14 @@ def cube_sphere(c, i, s, j, out):  # colliders.go:369-441
     vec_normalize(nrm)
     pen = r
     if not real_equal(dist, 0.0):
-        pen -= math.sqrt(dist)
+        pen -= sqrt_(dist)
     else:
         pen = 0.0
     out.append((i, j, cw, nrm, pen))
 
 
 def _try_axis(one, two, axis, to_center, index, smallest, case):  # colliders.go:445-477
-    if axis[0] * axis[0] + axis[1] * axis[1] + axis[2] * axis[2] < EPSILON:
+    if axis[0] * axis[0] + axis[1] * axis[1] + axis[2] * axis[2] < real_type(*axis)(EPSILON):
         return True, smallest, case
     axis = list(axis)
     vec_normalize(axis)
@@ -188,7 +189,7 @@ def _contact_point(p_one, d_one, one_size, p_two, d_two, two_size, use_one):  # 
     dp_sta_one = dot(d_one, to_st)
     dp_sta_two = dot(d_two, to_st)
     denom = sm_one * sm_two - dp_one_two * dp_one_two
-    if abs(denom) < EPSILON:
+    if abs(denom) < real_type(denom)(EPSILON):
         return list(p_one) if use_one else list(p_two)
     mua = (dp_one_two * dp_sta_two - sm_two * dp_sta_one) / denom
     mub = (sm_one * dp_sta_two - dp_one_two * dp_sta_one) / denom
@@ -202,7 +203,8 @@ def _contact_point(p_one, d_one, one_size, p_two, d_two, two_size, use_one):  # 
 def cube_cube(one, i, two, j, out):  # colliders.go:576-710
     c2, c1 = get_axis(two["T"], 3), get_axis(one["T"], 3)
     to_center = [c2[k] - c1[k] for k in range(3)]
-    pen, best = MAX_VALUE, 0xffffff
+    rt = real_type(*to_center)
+    pen, best = (np.finfo(np.float32).max if rt is np.float32 else MAX_VALUE), 0xffffff
     for k in range(3):
         ok, pen, best = _try_axis(one, two, get_axis(one["T"], k), to_center, k, pen, best)
         if not ok:

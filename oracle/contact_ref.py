@@ -12,8 +12,17 @@ contact sets and compares every bit.  Pure-Python loops: small worlds only.
 Vectors are lists of 3 floats, Matrix3 lists of 9 (column-major), Quat lists
 (w, x, y, z).  Bodies are dicts (see oracle/rigidbody_ref.py); a sleeping body
 needs its iit_body for the derived data that applyPositionChange refreshes.
+
+The same code also states the precision form (float32 with float64 islands):
+given numpy float32 values, every operation stays in float32 (Python float
+constants convert to float32 first, NumPy's scalar rules), and the islands
+convert to Python floats (float64) and back, where the precision form keeps
+float64: the friction solve's inversion and product, and the position and
+orientation accumulated across adjustPositions.
 """
 import math
+
+import numpy as np
 
 EPSILON = 1e-7
 EPSILON2 = EPSILON * EPSILON
@@ -23,13 +32,24 @@ POSITION_EPSILON = 0.01
 VELOCITY_EPSILON = 0.01
 
 
-def real_equal(a, b):  # math/math.go:64-78
+def real_type(*xs):
+    """np.float32 when any value is float32 (the precision form), else float."""
+    return np.float32 if any(isinstance(x, np.float32) for x in xs) else float
+
+
+def sqrt_(x):
+    return np.sqrt(x) if isinstance(x, np.float32) else math.sqrt(x)
+
+
+def real_equal(a, b):  # math/math.go:64-78, with the constants in the values' type
+    t = real_type(a, b)
+    eps = t(EPSILON)
     if a == b:
         return True
     diff = abs(a - b)
-    if a * b == 0 or diff < MIN_NORMAL:
-        return diff < EPSILON2
-    return diff / (abs(a) + abs(b)) < EPSILON
+    if a * b == 0 or diff < t(MIN_NORMAL):
+        return diff < eps * eps
+    return diff / (abs(a) + abs(b)) < eps
 
 
 # ---------------------------------------------------------------- vector.go
@@ -42,7 +62,7 @@ def dot(v, o):
 
 
 def magnitude(v):
-    return math.sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2])
+    return sqrt_(v[0] * v[0] + v[1] * v[1] + v[2] * v[2])
 
 
 def add(v, o):
@@ -151,11 +171,11 @@ class Contact:
 def _basis(c):  # contact.go:118-156
     n = c.normal
     if abs(n[0]) > abs(n[1]):
-        s = 1.0 / math.sqrt(n[2] * n[2] + n[0] * n[0])
+        s = 1.0 / sqrt_(n[2] * n[2] + n[0] * n[0])
         ty = [n[2] * s, 0.0, n[0] * -s]
         tz = [n[1] * ty[0], n[2] * ty[0] - n[0] * ty[2], -n[1] * ty[0]]
     else:
-        s = 1.0 / math.sqrt(n[2] * n[2] + n[1] * n[1])
+        s = 1.0 / sqrt_(n[2] * n[2] + n[1] * n[1])
         ty = [0.0, -n[2] * s, n[1] * s]
         tz = [n[1] * ty[2] - n[2] * ty[1], -n[0] * ty[2], n[0] * ty[1]]
     c.to_world = [n[0], n[1], n[2], ty[0], ty[1], ty[2], tz[0], tz[1], tz[2]]
@@ -256,12 +276,21 @@ def _apply_position_change(c, bodies, penetration):  # contact.go:286-386
             mul_with(ang_change[i], ang_m[i] / ang_i[i])
         lin_change[i] = list(c.normal)
         mul_with(lin_change[i], lin_m[i])
-        add_scaled(b["position"], c.normal, lin_m[i])
-        quat_add_scaled_vector(b["orientation"], ang_change[i], 1.0)
-        quat_normalize(b["orientation"])
+        # Position.AddScaled(normal, linearMove) and the orientation change,
+        # accumulated in float64 across the iterations (the precision form's
+        # island; plain float64 arithmetic in the float64 form)
+        t = real_type(lin_m[i])
+        pw, qw = b["position_w"], b["orientation_w"]
+        for k in range(3):
+            pw[k] += float(c.normal[k] * lin_m[i])
+        quat_add_scaled_vector(qw, [float(x) for x in ang_change[i]], 1.0)
+        quat_normalize(qw)
+        b["position"] = [t(x) for x in pw]
+        b["orientation"] = [t(x) for x in qw]
         if not b["awake"]:
             from oracle.rigidbody_ref import calculate_derived_data
             calculate_derived_data(b)
+            b["orientation_w"] = [float(x) for x in b["orientation"]]
     return lin_change, ang_change
 
 
@@ -285,10 +314,12 @@ def _friction_impulse(c, bodies, iits):  # contact.go:535-606
     dv[0] += inv_mass
     dv[4] += inv_mass
     dv[8] += inv_mass
-    k = m3_invert(dv)
-    kill = [c.desired, -c.velocity[1], -c.velocity[2]]
-    ic = m3_mul_vector(k, kill)
-    planar = math.sqrt(ic[1] * ic[1] + ic[2] * ic[2])
+    # the inversion and the product in float64 (the precision form's island)
+    t = real_type(dv[0])
+    k = m3_invert([float(x) for x in dv])
+    kill = [float(c.desired), float(-c.velocity[1]), float(-c.velocity[2])]
+    ic = [t(x) for x in m3_mul_vector(k, kill)]
+    planar = sqrt_(ic[1] * ic[1] + ic[2] * ic[2])
     if planar > ic[0] * c.friction:
         ic[1] /= planar
         ic[2] /= planar
@@ -347,6 +378,9 @@ def resolve_contacts(max_iterations, contacts, bodies, dt):
     adjustPositions and adjustVelocities."""
     if dt <= 0.0 or not contacts:
         return 0, 0
+    for b in bodies:
+        b["position_w"] = [float(x) for x in b["position"]]
+        b["orientation_w"] = [float(x) for x in b["orientation"]]
     for c in contacts:  # prepareContacts, contact.go:225-229
         _internals(c, bodies, dt)
     pos_used = 0  # adjustPositions, contact.go:233-283

@@ -8,12 +8,15 @@ narrowphase of oracle/colliders_ref.py, ResolveContacts of
 oracle/contact_ref.py), written from the Go source independently of the C++
 oracle.  Bodies are the dicts of those two modules plus acceleration, iit_body
 (the body-space inverse inertia, column-major), linear_damping,
-angular_damping, can_sleep and motion.
+angular_damping, can_sleep and motion.  With numpy float32 values it states
+the precision form (see oracle/contact_ref.py): the quaternion
+renormalisation is its float64 island here.
 """
 import math
 
 from oracle import colliders_ref, contact_ref
-from oracle.contact_ref import add_scaled, dot, m3_mul_vector, mul_with, quat_add_scaled_vector, quat_normalize
+from oracle.contact_ref import (add_scaled, dot, m3_mul_vector, mul_with, quat_add_scaled_vector, quat_normalize,
+                                real_type)
 
 SLEEP_EPSILON = 0.3  # rigidbody.go:14 (an untyped constant: 10 * it is exactly 3)
 
@@ -43,44 +46,54 @@ def transform_inertia_tensor(iit_body, t):  # rigidbody.go:275-299
 
 
 def calculate_derived_data(b):  # rigidbody.go:268-272
-    quat_normalize(b["orientation"])
+    q = b["orientation"]
+    rt = real_type(*q)
+    qw = [float(x) for x in q]  # the renormalisation in float64
+    quat_normalize(qw)
+    b["orientation"] = [rt(x) for x in qw]
     t = colliders_ref.set_as_transform(b["position"], b["orientation"])
     b["iit"] = transform_inertia_tensor(b["iit_body"], t)
 
 
 def set_awake(b, awake):  # rigidbody.go:182-192
+    rt = real_type(b["motion"])
     if awake:
         b["awake"] = True
-        b["motion"] = SLEEP_EPSILON * 2.0
+        b["motion"] = rt(SLEEP_EPSILON * 2.0)
     else:
         b["awake"] = False
-        b["velocity"] = [0.0, 0.0, 0.0]
-        b["rotation"] = [0.0, 0.0, 0.0]
+        b["velocity"] = [rt(0.0)] * 3
+        b["rotation"] = [rt(0.0)] * 3
 
 
 def integrate(b, dt):  # rigidbody.go:213-259, no forces or torques accumulated
+    """dt is the float64 frame time; the damping powers pow(d, dt) and the
+    sleep bias pow(0.5, dt) are taken in float64 and rounded to the bodies'
+    type, as the batch computes them once on the host."""
     if not b["awake"]:
         return
-    force, torque = [0.0, 0.0, 0.0], [0.0, 0.0, 0.0]
+    rt = real_type(b["inverse_mass"])
+    duration = rt(dt)
+    force, torque = [rt(0.0)] * 3, [rt(0.0)] * 3
     lfa = list(b["acceleration"])
     add_scaled(lfa, force, b["inverse_mass"])
     b["lfa"] = lfa
     ang_acc = m3_mul_vector(b["iit"], torque)
-    add_scaled(b["velocity"], lfa, dt)
-    add_scaled(b["rotation"], ang_acc, dt)
-    mul_with(b["velocity"], math.pow(b["linear_damping"], dt))
-    mul_with(b["rotation"], math.pow(b["angular_damping"], dt))
-    add_scaled(b["position"], b["velocity"], dt)
-    quat_add_scaled_vector(b["orientation"], b["rotation"], dt)
+    add_scaled(b["velocity"], lfa, duration)
+    add_scaled(b["rotation"], ang_acc, duration)
+    mul_with(b["velocity"], rt(math.pow(b["linear_damping"], dt)))
+    mul_with(b["rotation"], rt(math.pow(b["angular_damping"], dt)))
+    add_scaled(b["position"], b["velocity"], duration)
+    quat_add_scaled_vector(b["orientation"], b["rotation"], duration)
     calculate_derived_data(b)
     if b["can_sleep"]:
         current = dot(b["velocity"], b["velocity"]) + dot(b["rotation"], b["rotation"])
-        bias = math.pow(0.5, dt)
-        b["motion"] = bias * b["motion"] + (1.0 - bias) * current
-        if b["motion"] < SLEEP_EPSILON:
+        bias = rt(math.pow(0.5, dt))
+        b["motion"] = bias * b["motion"] + (rt(1.0) - bias) * current
+        if b["motion"] < rt(SLEEP_EPSILON):
             set_awake(b, False)
-        elif b["motion"] > 10 * SLEEP_EPSILON:
-            b["motion"] = 3.0
+        elif b["motion"] > rt(10 * SLEEP_EPSILON):
+            b["motion"] = rt(10 * SLEEP_EPSILON)
 
 
 def step(bodies, plane, dt, iter_mult=4):

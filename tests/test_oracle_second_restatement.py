@@ -7,7 +7,7 @@ import pytest
 
 from cubez_gb300 import scenes
 from oracle import contact_ref
-from oracle.oracle import FP64, OracleBatch
+from oracle.oracle import FP32, FP64, OracleBatch
 
 DT = 1.0 / 60.0
 
@@ -109,22 +109,28 @@ def test_narrowphase_matches_second_restatement(name, oracle_lib):
         assert (scenes.CUBE, scenes.SPHERE) in kinds
 
 
-def _frame_bodies(sc, w):
-    """The scene's bodies of world w as set up (CalculateDerivedData done)."""
+def _frame_bodies(sc, w, real=float):
+    """The scene's bodies of world w as set up (CalculateDerivedData done), in
+    the form's real type (the dampings stay float64: their powers are taken in
+    float64)."""
     from oracle import rigidbody_ref
     sl = sc.world_slice(w)
     offs = sc.collider_offset if sc.collider_offset is not None else np.tile(scenes.IDENTITY_OFFSET,
                                                                               (sc.num_bodies, 1))
+
+    def v(a):
+        return [real(x) for x in np.ravel(a)]
+
     bodies = []
     for i in range(sl.start, sl.stop):
-        b = {"shape": int(sc.shape[i]), "half": sc.half_size[i].tolist(), "radius": float(sc.radius[i]),
-             "position": sc.position[i].tolist(), "orientation": sc.orientation[i].tolist(),
-             "velocity": sc.velocity[i].tolist(), "rotation": sc.rotation[i].tolist(),
-             "acceleration": sc.acceleration[i].tolist(), "iit_body": sc.inverse_inertia[i].tolist(),
-             "inverse_mass": float(sc.inverse_mass[i]), "linear_damping": float(sc.linear_damping[i]),
+        b = {"shape": int(sc.shape[i]), "half": v(sc.half_size[i]), "radius": real(sc.radius[i]),
+             "position": v(sc.position[i]), "orientation": v(sc.orientation[i]),
+             "velocity": v(sc.velocity[i]), "rotation": v(sc.rotation[i]),
+             "acceleration": v(sc.acceleration[i]), "iit_body": v(sc.inverse_inertia[i]),
+             "inverse_mass": real(sc.inverse_mass[i]), "linear_damping": float(sc.linear_damping[i]),
              "angular_damping": float(sc.angular_damping[i]), "can_sleep": bool(sc.can_sleep[i]),
-             "awake": bool(sc.is_awake[i]), "lfa": [0.0, 0.0, 0.0], "offset": offs[i].tolist(),
-             "motion": float(sc.motion[i])}
+             "awake": bool(sc.is_awake[i]), "lfa": [real(0.0)] * 3, "offset": v(offs[i]),
+             "motion": real(sc.motion[i])}
         rigidbody_ref.calculate_derived_data(b)
         bodies.append(b)
     return bodies
@@ -149,8 +155,9 @@ FRAME_SCENES = {
 }
 
 
+@pytest.mark.parametrize("form", [FP64, FP32])
 @pytest.mark.parametrize("name", sorted(FRAME_SCENES))
-def test_frames_match_second_restatement(name, oracle_lib, monkeypatch):
+def test_frames_match_second_restatement(name, form, oracle_lib, monkeypatch):
     """Whole frames (Integrate, the ordered narrowphase, ResolveContacts) of
     the Python restatement against the oracle's step, every frame."""
     from oracle import rigidbody_ref
@@ -165,23 +172,25 @@ def test_frames_match_second_restatement(name, oracle_lib, monkeypatch):
     monkeypatch.setattr(rigidbody_ref, "set_awake", counting_set_awake)
     make, frames = FRAME_SCENES[name]
     sc = make()
-    o = OracleBatch(sc, form=FP64)
-    worlds = [_frame_bodies(sc, w) for w in range(sc.num_worlds)]
+    real = float if form == FP64 else np.float32
+    o = OracleBatch(sc, form=form)
+    worlds = [_frame_bodies(sc, w, real) for w in range(sc.num_worlds)]
+    plane = [real(x) for x in sc.plane]
     total = 0
     for fr in range(frames):
         o.step(1, DT)
         st, stats = o.bodies(), o.stats()
         for w, bodies in enumerate(worlds):
-            n, pit, vit = rigidbody_ref.step(bodies, sc.plane.tolist(), DT)
+            n, pit, vit = rigidbody_ref.step(bodies, plane, DT)
             assert (n, pit, vit) == (stats["contacts"][w], stats["pos_iterations"][w],
                                      stats["vel_iterations"][w]), (fr, w)
             total += n
             sl = sc.world_slice(w)
             for k in ("position", "orientation", "velocity", "rotation"):
-                got = np.array([b[k] for b in bodies])
+                got = np.array([b[k] for b in bodies], dtype=np.float64)
                 assert np.array_equal(got, st[k][sl]), "frame %d world %d: %s differs" % (fr, w, k)
-            assert np.array_equal(np.array([b["iit"] for b in bodies]), st["iit_world"][sl])
-            assert np.array_equal(np.array([b["motion"] for b in bodies]), st["motion"][sl])
+            assert np.array_equal(np.array([b["iit"] for b in bodies], dtype=np.float64), st["iit_world"][sl])
+            assert np.array_equal(np.array([b["motion"] for b in bodies], dtype=np.float64), st["motion"][sl])
             assert [int(b["awake"]) for b in bodies] == st["is_awake"][sl].tolist()
     assert total > 50
     if name == "sleeping":
