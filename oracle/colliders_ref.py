@@ -266,6 +266,23 @@ def check_for_collisions(one, i, two, j, out):  # colliders.go:720-747 (+ 209-21
         cube_cube(one, i, two, j, out)
 
 
+def collide_units(bodies, plane, units):
+    """A caller's test list in its order: (i, -1) is body i's
+    CheckAgainstHalfSpace, (i, j) CheckForCollisions(i, j)."""
+    for b in bodies:
+        b["T"] = collider_transform(b)
+    out = []
+    for i, j in units:
+        if j < 0:
+            if bodies[i]["shape"] == SPHERE:
+                sphere_half_space(bodies[i], i, plane, out)
+            else:
+                cube_half_space(bodies[i], i, plane, out)
+        else:
+            check_for_collisions(bodies[i], i, bodies[j], j, out)
+    return out
+
+
 def generate_contacts(bodies, plane):
     """examples/cubedrop.go:41-67: for each body the half-space test, then
     every other body in list order."""

@@ -96,13 +96,17 @@ def integrate(b, dt):  # rigidbody.go:213-259, no forces or torques accumulated
             b["motion"] = rt(10 * SLEEP_EPSILON)
 
 
-def step(bodies, plane, dt, iter_mult=4):
+def step(bodies, plane, dt, iter_mult=4, units=None):
     """One frame of examples/cubedrop.go:69-75 (with the batch's iteration
-    multiplier); returns (contacts, adjustPositions and adjustVelocities
-    iterations)."""
+    multiplier), or with `units` a caller's test list in place of the
+    all-pairs order (examples/ballistic.go:47-104); returns (contacts,
+    adjustPositions and adjustVelocities iterations)."""
     for b in bodies:
         integrate(b, dt)
-    found = colliders_ref.generate_contacts(bodies, plane)
+    if units is None:
+        found = colliders_ref.generate_contacts(bodies, plane)
+    else:
+        found = colliders_ref.collide_units(bodies, plane, units)
     contacts = [contact_ref.Contact(b0, b1, p, n, pen) for b0, b1, p, n, pen in found]
     pos_used, vel_used = contact_ref.resolve_contacts(len(contacts) * iter_mult, contacts, bodies, dt)
     return len(contacts), pos_used, vel_used

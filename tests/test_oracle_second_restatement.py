@@ -263,3 +263,34 @@ def test_frictionless_single_body_contact_is_the_nil_case(oracle_lib):
     assert status & 2  # the frictionless-nil bit
     with pytest.raises(contact_ref.NilBody):
         contact_ref.resolve_contacts(4 * len(fric), contacts, bodies, DT)
+
+
+@pytest.mark.parametrize("form", [FP64, FP32])
+def test_ballistic_frames_match_second_restatement(form, oracle_lib):
+    """examples/ballistic.go's loop (the example's test order, ResolveContacts
+    with len(contacts) * 8, the static backboard integrated as a static body)
+    frame by frame against the oracle."""
+    from oracle import rigidbody_ref
+    sc = scenes.ballistic(num_worlds=2, bullets=6, seed=77)
+    real = float if form == FP64 else np.float32
+    o = OracleBatch(sc, form=form)
+    units = scenes.ballistic_units(int(sc.counts[0]))
+    worlds = [_frame_bodies(sc, w, real) for w in range(sc.num_worlds)]
+    plane = [real(x) for x in sc.plane]
+    total = 0
+    for fr in range(150):
+        o.integrate(DT)
+        for w in range(sc.num_worlds):
+            o.collide(w, units)
+        o.resolve(DT, iter_mult=8)
+        st, stats = o.bodies(), o.stats()
+        for w, bodies in enumerate(worlds):
+            n, pit, vit = rigidbody_ref.step(bodies, plane, DT, iter_mult=8, units=units.tolist())
+            assert (n, pit, vit) == (stats["contacts"][w], stats["pos_iterations"][w],
+                                     stats["vel_iterations"][w]), (fr, w)
+            total += n
+            sl = sc.world_slice(w)
+            for k in ("position", "orientation", "velocity", "rotation"):
+                got = np.array([b[k] for b in bodies], dtype=np.float64)
+                assert np.array_equal(got, st[k][sl]), "frame %d world %d: %s differs" % (fr, w, k)
+    assert total > 50
