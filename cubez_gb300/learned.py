@@ -31,9 +31,16 @@ OFF_IS = OFF_MU + IN
 OFF_OS = OFF_IS + IN
 BLOB = OFF_OS + OUT
 
-FEATURES = ("normal_x", "normal_y", "normal_z", "cv_x", "cv_y", "cv_z", "penetration", "desired_dv",
-            "inv_mass_0", "inv_mass_1", "iw0_nn", "iw0_yy", "iw0_zz", "iw1_nn", "iw1_yy", "iw1_zz",
-            "contacts_body_0", "contacts_body_1")
+# The columns of the harvested features (contact_features in cz_resolve.cuh),
+# all in the contact basis: body 0's contacts with other bodies, a half-space
+# flag, the contact velocity, penetration, desired delta velocity, the
+# velocity-per-impulse matrix (nn, tt, ss, nt, ns, ts), the impulse that would
+# resolve the contact alone, and per body its contact count and the sum of its
+# contacts' positive desired delta velocities.
+FEATURES = ("body0_pair_contacts", "half_space", "cv_n", "cv_t", "cv_s", "penetration", "desired_dv",
+            "k_nn", "k_tt", "k_ss", "k_nt", "k_ns", "k_ts", "alone_impulse",
+            "contacts_body_0", "contacts_body_1", "load_body_0", "load_body_1")
+assert len(FEATURES) == IN
 
 
 def _ptr(a):
