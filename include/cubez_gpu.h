@@ -16,7 +16,9 @@
  *   RigidBody.CalculateDerivedData .. rigidbody.go:268-272  -> cz_upload_bodies
  *   Collider.CheckAgainst{HalfSpace,Sphere,Cube}, CheckForCollisions
  *                                     colliders.go:15-23, 178-710, 720-747
- *                                                           -> cz_narrowphase / cz_step
+ *                                                           -> cz_narrowphase / cz_step,
+ *                                                              cz_collide (a caller's order)
+ *   CollisionCube/Sphere.Offset ..... colliders.go:44,62    -> cz_bodies.collider_offset
  *   the per-frame loop of examples/cubedrop.go:29-75      -> cz_step
  *   ResolveContacts ................. contact.go:208-222    -> cz_resolve / cz_resolve_contacts
  *   Contact (exported fields) ....... contact.go:17-36      -> cz_contact
