@@ -293,21 +293,12 @@ void free_batch(cz_batch* b) {
   delete b;
 }
 
-int status_from_bits(uint32_t bits) {
-  if (bits & cz::ST_TIMEOUT) return CZ_ERR_TIMEOUT;
-  if (bits & cz::ST_NONFINITE) return CZ_ERR_NONFINITE;
-  if (bits & cz::ST_CAPACITY) return CZ_ERR_CAPACITY;
-  if (bits & cz::ST_BODY_LIMIT) return CZ_ERR_BODY_LIMIT;
-  if (bits & cz::ST_FRICTIONLESS_NIL) return CZ_ERR_FRICTIONLESS;
-  return CZ_OK;
-}
-
 // Synchronise the batch stream and turn the device status word into a cz_status.
 int finish(cz_batch* b) {
   CZ_CUDA(cudaMemcpyAsync(b->h_status, b->d_status, sizeof(uint32_t), cudaMemcpyDeviceToHost, b->stream));
   CZ_CUDA(cudaStreamSynchronize(b->stream));
   const uint32_t bits = *b->h_status;
-  const int st = status_from_bits(bits);
+  const int st = cz::status_from_bits(bits);
   if (st != CZ_OK) {
     char buf[96];
     std::snprintf(buf, sizeof buf, "device status bits 0x%x", bits);

@@ -6,6 +6,8 @@
 #include <cstddef>
 #include <cstdint>
 
+#include "../../include/cubez_gpu.h"
+#include "cz_layout.cuh"
 #include "cz_mlp.cuh"
 
 namespace cz {
@@ -117,5 +119,15 @@ cudaError_t mlp_pack(const float* dev_blob, unsigned char* dev_packed, cudaStrea
 
 // Records the message cz_last_error() returns; returns status.
 int set_error(int status, const char* what, cudaError_t e);
+
+// Device status bits (ST_*) -> the cz_status a call returns, most severe first.
+inline int status_from_bits(uint32_t bits) {
+  if (bits & ST_TIMEOUT) return CZ_ERR_TIMEOUT;
+  if (bits & ST_NONFINITE) return CZ_ERR_NONFINITE;
+  if (bits & ST_CAPACITY) return CZ_ERR_CAPACITY;
+  if (bits & ST_BODY_LIMIT) return CZ_ERR_BODY_LIMIT;
+  if (bits & ST_FRICTIONLESS_NIL) return CZ_ERR_FRICTIONLESS;
+  return CZ_OK;
+}
 
 }  // namespace cz

@@ -25,6 +25,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <cstdio>
 #include <mutex>
 
 #include "../../include/cubez_gpu.h"
@@ -276,8 +277,15 @@ int resolve_static(const cz::FormOps& ops, int32_t max_iterations, cz_contact* c
   if ((e = cudaMemcpyAsync(&bits, &m->status, sizeof bits, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
       (e = cudaStreamSynchronize(s)) != cudaSuccess)
     return cz::set_error(CZ_ERR_CUDA, "cz_resolve_contacts_static: status read-back", e);
-  if (bits & 0x80000000u) return CZ_ERR_BAD_ARG;
-  if (bits & cz::ST_FRICTIONLESS_NIL) return CZ_ERR_FRICTIONLESS;
+  if (bits & 0x80000000u)
+    return cz::set_error(CZ_ERR_BAD_ARG, "cz_resolve_contacts_static: a contact's body index is out of range",
+                         cudaSuccess);
+  const int st_bits = cz::status_from_bits(bits);
+  if (st_bits != CZ_OK) {
+    char buf[96];
+    std::snprintf(buf, sizeof buf, "cz_resolve_contacts_static: device status bits 0x%x", bits);
+    return cz::set_error(st_bits, buf, cudaSuccess);
+  }
   return CZ_OK;
 }
 

@@ -11,18 +11,31 @@ from tests import cases
 pytestmark = pytest.mark.gpu
 
 DT = 1.0 / 60.0
+_DT = {"is_awake": np.uint8, "can_sleep": np.uint8, "shape": np.int32}
 
 
-def _scene_with_contacts(seed=31):
-    """A settled mixed world and the contacts the narrowphase gives for it."""
-    sc = scenes.mixed(num_worlds=1, seed=seed, min_bodies=24, max_bodies=24)
-    ref = OracleBatch(sc)
-    ref.step(150, DT)
+def frame_state(scene, frames, form=0):
+    """The oracle `frames` frames into `scene`'s loop and then Integrate'd once
+    more: the body state ResolveContacts meets in the next frame of
+    examples/cubedrop.go:69-75, so the resolver has work.  Returns the oracle
+    batch (its last-frame accelerations and world inertia are the frame's) and
+    the moved scene."""
+    ref = OracleBatch(scene, form=form)
+    ref.step(frames, DT)
+    ref.integrate(DT)
     st = ref.bodies()
-    moved = sc.copy()
-    for k in ("position", "orientation", "velocity", "rotation"):
-        setattr(moved, k, st[k])
-    ref = OracleBatch(moved)
+    moved = scene.copy()
+    for k in ("position", "orientation", "velocity", "rotation", "motion", "is_awake"):
+        setattr(moved, k, np.array(st[k], dtype=_DT.get(k, np.float64), copy=True))
+    return ref, moved, st
+
+
+def scene_with_contacts(seed=31, bodies=24, frames=150, form=0):
+    """A mixed world mid-rollout and the contacts the narrowphase gives for it,
+    with the colliders' friction 0.9 and restitution 0.1."""
+    sc = scenes.mixed(num_worlds=1, seed=seed, min_bodies=bodies, max_bodies=bodies)
+    _, moved, _ = frame_state(sc, frames, form)
+    ref = OracleBatch(moved, form=form)
     ref.narrowphase()
     c = ref.contacts(0)
     c["friction"] = np.full(len(c["penetration"]), 0.9)
@@ -30,7 +43,13 @@ def _scene_with_contacts(seed=31):
     return moved, c
 
 
-def _cz_contacts(c):
+def host_arrays(scene):
+    """Fresh copies of the scene's body arrays: the entry points write their
+    results back in place, and the oracle must start from the untouched scene."""
+    return {k: np.array(getattr(scene, k), dtype=_DT.get(k, np.float64), copy=True) for k in scene.FIELDS}
+
+
+def cz_contacts(c):
     from cubez_gb300 import _lib
     n = len(c["penetration"])
     arr = (_lib.Contact * n)()
@@ -44,60 +63,107 @@ def _cz_contacts(c):
     return arr
 
 
-def _resolve_both(scene, c, max_iterations, form=0):
+def resolve_both(scene, c, max_iterations, form=0, ref=None, extra=None):
+    """cz_resolve_contacts on copies of the scene's arrays, and the oracle's
+    ResolveContacts on the same contacts.  `ref` is an oracle batch holding the
+    same state (default: a fresh one built from the scene, whose last-frame
+    accelerations are zero, as a NULL last_frame_acceleration is); `extra`
+    adds optional body arrays (last_frame_acceleration, inverse_inertia_world)."""
     import ctypes as C
 
-    from cubez_gb300 import _lib
     from cubez_gb300.batch import WorldBatch, bodies_struct
     gpu = WorldBatch(scene.counts, form=form, plane=scene.plane)
-    n = scene.num_bodies
-    arrays = {k: np.ascontiguousarray(getattr(scene, k), dtype={"is_awake": np.uint8, "can_sleep": np.uint8,
-                                                              "shape": np.int32}.get(k, np.float64))
-              for k in scene.FIELDS}
+    arrays = host_arrays(scene)
     arrays["inverse_inertia_world"] = None
+    for k, v in (extra or {}).items():
+        arrays[k] = np.array(v, dtype=np.float64, copy=True)
     s = bodies_struct(arrays)
-    arr = _cz_contacts(c)
+    arr = cz_contacts(c)
     st = gpu.L.cz_resolve_contacts(gpu.h, max_iterations, C.cast(arr, C.c_void_p), len(arr), DT, C.byref(s))
-    ref = OracleBatch(scene, form=form)
+    gpu.close()
+    if ref is None:
+        ref = OracleBatch(scene, form=form)
     ref.set_contacts(0, c)
-    ref.resolve_fixed(max_iterations, DT)
-    return st, arrays, arr, ref, n
+    assert ref.resolve_fixed(max_iterations, DT) == 0
+    return st, arrays, arr, ref
+
+
+def assert_matches_oracle(arrays, arr, ref, fields=("position", "orientation", "velocity", "rotation")):
+    r = ref.bodies()
+    for k in fields:
+        np.testing.assert_array_equal(arrays[k], r[k], err_msg=k)
+    rc = ref.resolved_contacts(0)
+    n = len(arr)
+    np.testing.assert_array_equal(np.array([arr[i].penetration for i in range(n)]), rc["penetration"])
+    np.testing.assert_array_equal(np.array([list(arr[i].normal) for i in range(n)]), rc["normal"])
+    np.testing.assert_array_equal(np.array([list(arr[i].body) for i in range(n)]), rc["bodies"])
 
 
 @pytest.mark.parametrize("form", [0, 1])
-def test_resolve_contacts_matches_oracle(form, cuda_lib):
-    scene, c = _scene_with_contacts()
-    assert len(c["penetration"]) > 20
-    st, arrays, arr, ref, n = _resolve_both(scene, c, 4 * len(c["penetration"]), form)
-    assert st == 0
-    r = ref.bodies()
-    for k in ("position", "orientation", "velocity", "rotation"):
-        np.testing.assert_array_equal(arrays[k], r[k])
-    rc = ref.resolved_contacts(0)
-    pen = np.array([arr[i].penetration for i in range(len(arr))])
-    np.testing.assert_array_equal(pen, rc["penetration"])
+@pytest.mark.parametrize("seed,bodies,frames", [(31, 24, 150), (41, 64, 150)])
+def test_resolve_contacts_matches_oracle(form, seed, bodies, frames, cuda_lib):
+    scene, c = scene_with_contacts(seed, bodies, frames, form)
+    n = len(c["penetration"])
+    assert n > 20
+    st, arrays, arr, ref = resolve_both(scene, c, 4 * n, form)
+    assert st == 0, cuda_lib.cz_last_error()
+    s = ref.stats()
+    assert s["pos_iterations"][0] > 0 and s["vel_iterations"][0] > 0   # the resolver had work
+    assert_matches_oracle(arrays, arr, ref)
+
+
+@pytest.mark.parametrize("form", [0, 1])
+def test_resolve_contacts_with_frame_inputs(form, cuda_lib):
+    """last_frame_acceleration (the restitution and local-velocity terms of
+    contact.go:87-112,159-182) and an explicit world inverse inertia, as a
+    frame loop passes them after Integrate: the oracle that integrated the
+    frame against the entry point given that frame's values."""
+    sc = scenes.mixed(num_worlds=1, seed=32, min_bodies=24, max_bodies=24)
+    ref, moved, st = frame_state(sc, 150, form)
+    ref.narrowphase()
+    c = ref.contacts(0)
+    n = len(c["penetration"])
+    c["friction"] = np.full(n, 0.9)
+    c["restitution"] = np.full(n, 0.1)
+    # Integrate sets lastFrameAccelleration = Acceleration + forceAccum * inverseMass
+    # (rigidbody.go:222-223) with no force applied
+    extra = {"last_frame_acceleration": moved.acceleration, "inverse_inertia_world": st["iit_world"]}
+    stt, arrays, arr, ref = resolve_both(moved, c, 4 * n, form, ref=ref, extra=extra)
+    assert stt == 0, cuda_lib.cz_last_error()
+    assert ref.stats()["vel_iterations"][0] > 0
+    assert_matches_oracle(arrays, arr, ref)
+    # the accelerations matter: without them the result differs
+    st0, arrays0, _, _ = resolve_both(moved, c, 4 * n, form, ref=OracleBatch(moved, form=form))
+    assert not np.array_equal(arrays0["velocity"], arrays["velocity"])
 
 
 def test_resolve_contacts_swaps_nil_first_body(cuda_lib):
     scene = cases.cube_resting()
     c = {"bodies": np.array([[-1, 0]], np.int32), "point": np.array([[0.5, -0.02, 0.5]]),
-         "normal": np.array([[0.0, -1.0, 0.0]]), "penetration": np.array([0.01]),
+         "normal": np.array([[0.0, -1.0, 0.0]]), "penetration": np.array([0.02]),
          "friction": np.array([0.9]), "restitution": np.array([0.1])}
-    st, arrays, arr, ref, n = _resolve_both(scene, c, 4, 0)
+    st, arrays, arr, ref = resolve_both(scene, c, 4, 0)
     assert st == 0
     assert list(arr[0].body) == [0, -1]          # calculateInternals, contact.go:61-65
     assert list(arr[0].normal) == [0.0, 1.0, 0.0]
-    r = ref.bodies()
-    np.testing.assert_array_equal(arrays["position"], r["position"])
-    np.testing.assert_array_equal(arrays["velocity"], r["velocity"])
+    assert ref.stats()["pos_iterations"][0] > 0
+    assert_matches_oracle(arrays, arr, ref)
 
 
 def test_resolve_contacts_zero_iterations_and_guards(cuda_lib):
-    scene, c = _scene_with_contacts(seed=32)
-    st, arrays, arr, ref, n = _resolve_both(scene, c, 0, 0)
+    scene, c = scene_with_contacts(seed=32)
+    n = len(c["penetration"])
+    # the same contacts need iterations when allowed some
+    ref = OracleBatch(scene)
+    ref.set_contacts(0, c)
+    ref.resolve_fixed(4 * n, DT)
+    assert ref.stats()["pos_iterations"][0] > 0
+    st, arrays, arr, ref = resolve_both(scene, c, 0, 0)
     assert st == 0
-    # no iteration: positions unchanged (prepareContacts alone mutates no body)
-    np.testing.assert_array_equal(arrays["position"], scene.position)
+    # no iteration: no body moves (prepareContacts alone mutates no body)
+    for k in ("position", "orientation", "velocity", "rotation"):
+        np.testing.assert_array_equal(arrays[k], getattr(scene, k))
+    assert_matches_oracle(arrays, arr, ref)
 
 
 def test_capacity_overflow_is_reported(cuda_lib):
@@ -146,7 +212,7 @@ def test_bad_arguments_on_a_live_batch(cuda_lib):
     assert b.L.cz_set_tuning(b.h, C.byref(t)) == 1  # large-world lanes must be 16 or 32
     bad = {"bodies": np.array([[0, 7]], np.int32), "point": np.zeros((1, 3)), "normal": np.array([[1.0, 0, 0]]),
            "penetration": np.array([0.1]), "friction": np.array([0.9]), "restitution": np.array([0.1])}
-    arr = _cz_contacts(bad)
+    arr = cz_contacts(bad)
     from cubez_gb300.batch import bodies_struct
     s = bodies_struct({k: getattr(scene, k) for k in scene.FIELDS})
     assert b.L.cz_resolve_contacts(b.h, 4, C.cast(arr, C.c_void_p), 1, DT, C.byref(s)) == 1

@@ -7,49 +7,22 @@ library's scratch is its statically reserved array.
 Checked against the allocating entry point cz_resolve_contacts on the same
 inputs, bit for bit (the tolerance of every parity test in this suite), on two
 calls in a row so that the second call starts from the scratch contents the
-first one left behind.  Last, both entry points with per-contact friction and
-restitution against the oracle."""
+first one left behind, and against the oracle directly.  Every world here is
+taken mid-rollout, after an Integrate, so the resolver iterates.  Last, both
+entry points with per-contact friction and restitution against the oracle."""
 import ctypes as C
 
 import numpy as np
 import pytest
 
 from cubez_gb300 import scenes
+from tests.test_gpu_api import (assert_matches_oracle, cz_contacts, frame_state, host_arrays, resolve_both,
+                                scene_with_contacts)
 
 pytestmark = pytest.mark.gpu
 
 DT = 1.0 / 60.0
-_DT = {"is_awake": np.uint8, "can_sleep": np.uint8, "shape": np.int32}
-
-
-def _settled_world(seed, bodies):
-    from oracle.oracle import OracleBatch
-    sc = scenes.mixed(num_worlds=1, seed=seed, min_bodies=bodies, max_bodies=bodies)
-    ref = OracleBatch(sc)
-    ref.step(150, DT)
-    st = ref.bodies()
-    moved = sc.copy()
-    for k in ("position", "orientation", "velocity", "rotation"):
-        setattr(moved, k, st[k])
-    ref = OracleBatch(moved)
-    ref.narrowphase()
-    c = ref.contacts(0)
-    n = len(c["penetration"])
-    return moved, c, n
-
-
-def _contact_array(c):
-    from cubez_gb300 import _lib
-    n = len(c["penetration"])
-    arr = (_lib.Contact * n)()
-    for i in range(n):
-        arr[i].body[0], arr[i].body[1] = int(c["bodies"][i][0]), int(c["bodies"][i][1])
-        arr[i].friction, arr[i].restitution = 0.9, 0.1
-        for k in range(3):
-            arr[i].point[k] = float(c["point"][i][k])
-            arr[i].normal[k] = float(c["normal"][i][k])
-        arr[i].penetration = float(c["penetration"][i])
-    return arr
+_OPTIONAL = ("last_frame_acceleration", "inverse_inertia_world")
 
 
 def _contacts_np(arr):
@@ -58,33 +31,19 @@ def _contacts_np(arr):
     return raw.copy()
 
 
-def _host_arrays(scene):
-    """Fresh copies: both entry points write their results back in place."""
-    return {k: np.array(getattr(scene, k), dtype=_DT.get(k, np.float64), copy=True) for k in scene.FIELDS}
-
-
-def _with_existing_entry_point(scene, arr, form):
-    """The allocating entry point, on host arrays."""
-    from cubez_gb300.batch import WorldBatch, bodies_struct
-    b = WorldBatch(scene.counts, form=form, plane=scene.plane)
-    host = _host_arrays(scene)
-    s = bodies_struct(host)
-    st = b.L.cz_resolve_contacts(b.h, 4 * len(arr), C.cast(arr, C.c_void_p), len(arr), DT, C.byref(s))
-    b.close()
-    return st, host
-
-
-def _with_static_entry_point(lib, scene, arr, form):
+def _with_static_entry_point(lib, scene, arr, form, extra=None):
     """The allocation-free entry point, on device buffers the caller owns."""
     import torch
     from cubez_gb300 import _lib
-    host = _host_arrays(scene)
+    host = host_arrays(scene)
+    for k, v in (extra or {}).items():
+        host[k] = np.array(v, dtype=np.float64, copy=True)
     dev = {k: torch.from_numpy(v.copy()).cuda() for k, v in host.items()}
     raw = _contacts_np(arr)
     dcontacts = torch.from_numpy(raw.view(np.uint8).copy()).cuda()
     s = _lib.Bodies()
     for name in ("position", "orientation", "velocity", "rotation", "acceleration", "inverse_inertia",
-                 "inverse_mass", "motion", "is_awake"):
+                 "inverse_mass", "motion", "is_awake") + tuple(k for k in _OPTIONAL if k in dev):
         setattr(s, name, C.c_void_p(dev[name].data_ptr()))
     torch.cuda.synchronize()
     st = lib.cz_resolve_contacts_static(form, 4 * len(arr), C.c_void_p(dcontacts.data_ptr()), len(arr), DT,
@@ -103,23 +62,56 @@ def _compare(host, arr_after, out, out_contacts):
     np.testing.assert_array_equal(out_contacts["body"], ref["body"])
 
 
+def _static_against_oracle(out, out_contacts, ref):
+    r = ref.bodies()
+    for k in ("position", "orientation", "velocity", "rotation"):
+        np.testing.assert_array_equal(out[k], r[k], err_msg=k)
+    rc = ref.resolved_contacts(0)
+    np.testing.assert_array_equal(out_contacts["penetration"], rc["penetration"])
+    np.testing.assert_array_equal(out_contacts["normal"], rc["normal"])
+    np.testing.assert_array_equal(out_contacts["body"], rc["bodies"])
+
+
 @pytest.mark.parametrize("form", [0, 1])
 def test_static_scratch_matches_existing_entry_point_twice(form, cuda_lib):
-    # first call: a large world whose contacts exceed the shared-memory tile
+    # first call: a 64-body world whose contacts exceed the shared-memory tile
     # (they use the working rows in the static scratch); second call: a small
     # world, starting from the scratch the first call left behind
     for seed, bodies in ((41, 64), (42, 20)):
-        scene, c, n = _settled_world(seed, bodies)
-        assert n > 0
+        scene, c = scene_with_contacts(seed, bodies, 150, form)
+        n = len(c["penetration"])
         if bodies == 64:
             assert n > 128
-        arr_a = _contact_array(c)
-        arr_b = _contact_array(c)
-        st_a, host = _with_existing_entry_point(scene, arr_a, form)
-        st_b, out, out_contacts = _with_static_entry_point(cuda_lib, scene, arr_b, form)
-        assert st_a == 0
+        st_a, host, arr_a, ref = resolve_both(scene, c, 4 * n, form)
+        assert st_a == 0, cuda_lib.cz_last_error()
+        assert ref.stats()["pos_iterations"][0] > 0 and ref.stats()["vel_iterations"][0] > 0
+        assert_matches_oracle(host, arr_a, ref)
+        st_b, out, out_contacts = _with_static_entry_point(cuda_lib, scene, cz_contacts(c), form)
         assert st_b == 0, cuda_lib.cz_last_error()
         _compare(host, arr_a, out, out_contacts)
+        _static_against_oracle(out, out_contacts, ref)
+
+
+@pytest.mark.parametrize("form", [0, 1])
+def test_static_scratch_with_frame_inputs(form, cuda_lib):
+    """The optional inputs a frame loop passes after Integrate: last-frame
+    accelerations and the world inverse inertia, against the oracle that
+    integrated that frame and against the allocating entry point."""
+    sc = scenes.mixed(num_worlds=1, seed=32, min_bodies=24, max_bodies=24)
+    ref, moved, st = frame_state(sc, 150, form)
+    ref.narrowphase()
+    c = ref.contacts(0)
+    n = len(c["penetration"])
+    c["friction"] = np.full(n, 0.9)
+    c["restitution"] = np.full(n, 0.1)
+    extra = {"last_frame_acceleration": moved.acceleration, "inverse_inertia_world": st["iit_world"]}
+    st_a, host, arr_a, ref = resolve_both(moved, c, 4 * n, form, ref=ref, extra=extra)
+    assert st_a == 0, cuda_lib.cz_last_error()
+    assert ref.stats()["vel_iterations"][0] > 0
+    st_b, out, out_contacts = _with_static_entry_point(cuda_lib, moved, cz_contacts(c), form, extra)
+    assert st_b == 0, cuda_lib.cz_last_error()
+    _compare(host, arr_a, out, out_contacts)
+    _static_against_oracle(out, out_contacts, ref)
 
 
 def test_static_scratch_rejects_sizes_beyond_its_maximum(cuda_lib):
@@ -138,16 +130,15 @@ def test_resolve_contacts_with_contact_materials(form, cuda_lib):
     restitution in [0, 0.6].  The allocating entry point against the oracle,
     and the allocation-free one against it, bit for bit."""
     from oracle.oracle import OracleBatch
-    from tests.test_gpu_api import _resolve_both
     # a 3 x 3 x 2 pile one second after the drop: 50 contacts, 24 between cubes
     scene = scenes.piles(num_worlds=1, seed=76, nx=3, nz=3, ny=2, spacing=1.1)
-    ref = OracleBatch(scene)
+    ref = OracleBatch(scene, form=form)
     ref.step(60, DT)
     st = ref.bodies()
     scene = scene.copy()
     for k in ("position", "orientation", "velocity", "rotation"):
-        setattr(scene, k, st[k])
-    ref = OracleBatch(scene)
+        setattr(scene, k, np.array(st[k], copy=True))
+    ref = OracleBatch(scene, form=form)
     ref.narrowphase()
     c = ref.contacts(0)
     n = len(c["penetration"])
@@ -156,18 +147,11 @@ def test_resolve_contacts_with_contact_materials(form, cuda_lib):
     c["friction"] = np.where(two, 0.0, rng.uniform(0.2, 1.0, n))
     c["restitution"] = rng.uniform(0.0, 0.6, n)
     assert two.sum() > 10 and (~two).sum() > 10
-    st, arrays, arr, ref, _ = _resolve_both(scene, c, 4 * n, form)
+    st, arrays, arr, ref = resolve_both(scene, c, 4 * n, form)
     assert st == 0, cuda_lib.cz_last_error()
     assert ref.stats()["vel_iterations"][0] > 20
-    r = ref.bodies()
-    for k in ("position", "orientation", "velocity", "rotation"):
-        np.testing.assert_array_equal(arrays[k], r[k], err_msg=k)
-    rc = ref.resolved_contacts(0)
-    np.testing.assert_array_equal(np.array([arr[i].penetration for i in range(n)]), rc["penetration"])
+    assert_matches_oracle(arrays, arr, ref)
     # the allocation-free entry point on the same materials
-    from tests.test_gpu_api import _cz_contacts
-    arr_s = _cz_contacts(c)
-    st_s, out, out_contacts = _with_static_entry_point(cuda_lib, scene, arr_s, form)
+    st_s, out, out_contacts = _with_static_entry_point(cuda_lib, scene, cz_contacts(c), form)
     assert st_s == 0, cuda_lib.cz_last_error()
-    for k in ("position", "orientation", "velocity", "rotation"):
-        np.testing.assert_array_equal(out[k], arrays[k], err_msg=k)
+    _static_against_oracle(out, out_contacts, ref)
