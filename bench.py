@@ -219,20 +219,27 @@ def run_ours(args):
         torch.cuda.synchronize()
 
     from cubez_gb300 import autotune, learned
-    t0 = time.perf_counter()
-    blob, train_info = learned.train_warm_start(num_worlds=args.train_worlds, device=local)
-    train_info["seconds"] = time.perf_counter() - t0
-
     forms = [("fp32_mlp", FORM_FP32), ("fp32", FORM_FP32), ("fp64", FORM_FP64)]
     if args.fp32_only:
         forms = forms[:2]
+    if args.forms:
+        forms = [f for f in forms if f[0] in args.forms.split(",")]
+    train_info = None
+    if any(name == "fp32_mlp" for name, _ in forms):
+        t0 = time.perf_counter()
+        blob, train_info = learned.train_warm_start(num_worlds=args.train_worlds, device=local)
+        train_info["seconds"] = time.perf_counter() - t0
+    fixed = json.loads(args.tuning) if args.tuning else None
     batches = {}
     tuning = {}
     for name, form in forms:
         b = WorldBatch.from_scene(scene, form=form, device=local)
         if name == "fp32_mlp":
             learned.set_warm_start(b, blob)
-        if args.autotune:
+        if fixed:
+            b.set_tuning(**fixed)
+            tuning[name] = b.get_tuning()
+        elif args.autotune:
             # tune on a settled state (half-way through the rollout), untimed
             b.step(frames // 2, DT)
             b.snapshot()
@@ -277,10 +284,11 @@ def run_ours(args):
                          "launches": launches, "clocks": clocks.summary(), "steps": steps, "warmup": warmup,
                          "value": nb * frames * ws / (ms / 1e3)}
 
+    head = "fp32_mlp" if "fp32_mlp" in results else forms[0][0]
     # e2e through the C ABI with host buffers (the headline form)
     e2e = None
     if not args.no_e2e:
-        b = batches["fp32_mlp"]
+        b = batches[head]
         host = {k: np.ascontiguousarray(getattr(scene, k)) for k in scene.FIELDS}
         import ctypes as C
         pinned = {}
@@ -310,8 +318,8 @@ def run_ours(args):
 
     acc = accuracy(scene, frames, batches) if not args.no_accuracy and "fp64" in batches else None
 
-    r32 = results["fp32_mlp"]
-    real = 4
+    r32 = results[head]
+    real = 4 if batches[head].form == FORM_FP32 else 8
     phase_names = ["integrate", "narrowphase", "resolve"]
     ph = r32["phase_ms"]
     dom = int(np.argmax(ph))
@@ -325,7 +333,7 @@ def run_ours(args):
         pl = ph[i] / frames
         kernels[n] = {"ms_per_launch": pl, "share": ph[i] / sum(ph), "alg_bytes_per_launch": bl,
                       "gbs": bl / (pl / 1e3) / 1e9}
-    info = batches["fp32_mlp"].info()
+    info = batches[head].info()
     for b in batches.values():
         b.close()
 
@@ -348,7 +356,8 @@ def run_ours(args):
         "vs_baseline": None, "dtype": "f32 (f64 islands) + bf16 MLP", "data": "synthetic (seeded scenes)",
         "config": {"workload": "precision: %d worlds x %d bodies (16 spheres + 16 cubes), %d-frame rollout, "
                                "dt=1/60, iterations 4 x contacts" % (args.worlds, args.bodies, frames),
-                   "form": "fp32 + learned warm start (18-64-64-64-3 BF16 MLP on tensor cores)",
+                   "form": {"fp32_mlp": "fp32 + learned warm start (18-64-64-64-3 BF16 MLP on tensor cores)",
+                            "fp32": "fp32 (f64 islands), plain resolver", "fp64": "fp64, bit-exact"}[head],
                    "step": "one %d-frame rollout" % frames,
                    "l2": "explicit 252 MB flush before every timed rollout; working set > L2",
                    "parallelism": "weak: %d worlds per GPU" % args.worlds},
@@ -356,8 +365,8 @@ def run_ours(args):
         "fp64": block("fp64"),
         "mlp_over_fp64": (r32["value"] / fp64v) if fp64v else None,
         "fp32_plain_over_fp64": (results["fp32"]["value"] / fp64v) if fp64v else None,
-        "mlp_over_fp32_plain": r32["value"] / results["fp32"]["value"],
-        "warm_start": {"training": train_info,
+        "mlp_over_fp32_plain": (r32["value"] / results["fp32"]["value"]) if "fp32" in results else None,
+        "warm_start": None if train_info is None else {"training": train_info,
                        "policy": "worlds whose previous solve used at most 1/%d of the iteration budget are "
                                  "warm-started (warm_start_budget_shift %d); the tuner does not change it"
                                  % (1 << tuning.get("fp32_mlp", {}).get("warm_start_budget_shift", 2),
@@ -366,7 +375,8 @@ def run_ours(args):
                        "warm_bodies_per_frame": cnt["warm_bodies"] / (frames * args.steps),
                        "mean_scale": cnt["warm_scale_sum"] / max(1, cnt["warm_bodies"]),
                        "fallbacks_per_frame": cnt["warm_fallbacks"] / (frames * args.steps),
-                       "vel_iterations_vs_plain": cnt["vel_iterations"] / max(1, results["fp32"]["counters"]["vel_iterations"])},
+                       "vel_iterations_vs_plain": cnt["vel_iterations"] / max(
+                           1, results["fp32"]["counters"]["vel_iterations"]) if "fp32" in results else None},
         "accuracy": acc,
         "e2e": e2e,
         "gpu_launches": r32["launches"],
@@ -559,6 +569,8 @@ def main():
     ap.add_argument("--fp64-steps", type=int, default=1)
     ap.add_argument("--fp64-warmup", type=int, default=1)
     ap.add_argument("--fp32-only", action="store_true")
+    ap.add_argument("--forms", default="", help="comma-separated subset of fp32_mlp,fp32,fp64")
+    ap.add_argument("--tuning", default="", help="fixed tuning knobs as JSON (skips the autotuner)")
     ap.add_argument("--autotune", type=int, default=1)
     ap.add_argument("--tune-frames", type=int, default=30)
     ap.add_argument("--no-e2e", action="store_true")

@@ -20,7 +20,7 @@ class OrcBodies(C.Structure):
     _fields_ = [(name, C.c_void_p) for name in (
         "position", "orientation", "velocity", "rotation", "acceleration", "inverse_inertia", "inverse_mass",
         "linear_damping", "angular_damping", "motion", "is_awake", "can_sleep", "shape", "half_size", "radius",
-        "collider_offset")]
+        "collider_offset", "last_frame_acceleration")]
 
 
 def lib():
@@ -84,7 +84,9 @@ def _bodies_struct(arrays):
 class OracleBatch:
     """A batch of independent worlds stepped on the CPU by the oracle."""
 
-    def __init__(self, scene, form=FP64):
+    def __init__(self, scene, form=FP64, last_frame_acceleration=None):
+        """`last_frame_acceleration` ([n, 3]): the bodies' lastFrameAccelleration
+        at setup (default zero, as NewRigidBody leaves it)."""
         self.L = lib()
         self.scene = scene
         self.form = form
@@ -92,6 +94,8 @@ class OracleBatch:
                       for k in scene.FIELDS}
         if getattr(scene, "collider_offset", None) is not None:
             self._keep["collider_offset"] = np.ascontiguousarray(scene.collider_offset, dtype=np.float64)
+        if last_frame_acceleration is not None:
+            self._keep["last_frame_acceleration"] = np.ascontiguousarray(last_frame_acceleration, dtype=np.float64)
         s = _bodies_struct(self._keep)
         self.h = self.L.orc_create(form, scene.num_worlds, _ptr(scene.counts), C.byref(s), _ptr(scene.plane))
 

@@ -32,6 +32,7 @@ struct orc_bodies {
   double* half_size;        // [n][3]
   double* radius;           // [n]
   double* collider_offset;  // [n][12] collider Offset (column-major 3x4), null = identity
+  double* last_frame_acceleration;  // [n][3] lastFrameAccelleration at setup, null = zero (as NewRigidBody)
 };
 }
 
@@ -104,6 +105,8 @@ template <class R, class W> struct Batch : BatchBase {
       // (examples/cubedrop.go:171-172).
       CalculateDerivedData(b);
       ColliderDerivedData(b);
+      if (in->last_frame_acceleration)
+        for (int k = 0; k < 3; ++k) b.lastFrameAccel[k] = (R)in->last_frame_acceleration[3 * i + k];
     }
     for (int k = 0; k < 3; ++k) plane.normal[k] = (R)plane4[k];
     plane.offset = (R)plane4[3];

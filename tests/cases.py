@@ -76,6 +76,40 @@ def cube_edge_edge():
                  FAR_PLANE)
 
 
+def _qmul(a, b):
+    w1, x1, y1, z1 = a
+    w2, x2, y2, z2 = b
+    return np.array([w1 * w2 - x1 * x2 - y1 * y2 - z1 * z2, w1 * x2 + x1 * w2 + y1 * z2 - z1 * y2,
+                     w1 * y2 - x1 * z2 + y1 * w2 + z1 * x2, w1 * z2 + x1 * y2 - y1 * x2 + z1 * w2])
+
+
+def cube_edge_edge_near_parallel(twist, yaw):
+    """Two unit cubes turned 45 deg about z, one on the other edge to edge
+    (0.03 deep), the upper one twisted by `twist` about the vertical and both
+    turned by `yaw` about it: the cross product of the two edges is tiny, so
+    the edge-edge axis is the best one while the edges are almost parallel
+    and contactPoint (colliders.go:519-573) meets a denominator near its
+    epsilon.  Whether it takes the parallel or the out-of-range fallback, or
+    crosses the edges, depends on the rounding of the form's arithmetic."""
+    spin = quat_axis(math.pi / 4, (0.0, 0.0, 1.0))
+    turn = quat_axis(yaw, (0.0, 1.0, 0.0))
+    qa = _qmul(turn, spin)
+    qb = _qmul(turn, _qmul(quat_axis(twist, (0.0, 1.0, 0.0)), spin))
+    d = math.sqrt(2.0)
+    return world([dict(shape="cube", pos=(0.0, 5.0, 0.0), half=(0.5, 0.5, 0.5), quat=qa),
+                  dict(shape="cube", pos=(0.0, 5.0 + d - 0.03, 0.0), half=(0.5, 0.5, 0.5), quat=qb)], FAR_PLANE)
+
+
+def edge_parallel_fallback():
+    # in the precision form, |denom| < epsilon: contactPoint returns an edge's midpoint
+    return cube_edge_edge_near_parallel(0.0005068890466341242, 3.143832173958728)
+
+
+def edge_range_fallback():
+    # in the precision form, the closest points fall outside the edges: an edge's midpoint again
+    return cube_edge_edge_near_parallel(0.000588497158099136, 4.553989506659829)
+
+
 def tilted_cube_on_plane():
     # one vertex down: a single plane contact
     q = quat_axis(math.atan(math.sqrt(2.0)), (1.0, 0.0, -1.0))
@@ -109,4 +143,5 @@ ALL = {"cube_resting": cube_resting, "sphere_resting": sphere_resting, "sphere_p
        "cube_sphere": cube_sphere, "sphere_inside_cube": sphere_inside_cube, "cube_on_cube": cube_on_cube,
        "cube_edge_edge": cube_edge_edge, "tilted_cube_on_plane": tilted_cube_on_plane,
        "cube_edge_down": cube_edge_down, "cube_below_plane": cube_below_plane,
-       "static_cube_singular_friction": static_cube_singular_friction}
+       "static_cube_singular_friction": static_cube_singular_friction,
+       "edge_parallel_fallback": edge_parallel_fallback, "edge_range_fallback": edge_range_fallback}

@@ -112,28 +112,41 @@ def test_resolve_contacts_matches_oracle(form, seed, bodies, frames, cuda_lib):
     assert_matches_oracle(arrays, arr, ref)
 
 
+def frame_inputs(form, seed=32):
+    """A world mid-rollout with the optional inputs a frame loop passes after
+    Integrate: lastFrameAccelleration = Acceleration + forceAccum * inverseMass
+    (rigidbody.go:222-223), here gravity plus a horizontal push so that its
+    tangential part reaches the contact velocities (contact.go:172-180), and
+    the world inverse inertia.  Returns the scene, the contacts, the optional
+    arrays and an oracle batch holding the same state."""
+    sc = scenes.mixed(num_worlds=1, seed=seed, min_bodies=24, max_bodies=24)
+    _, moved, st = frame_state(sc, 150, form)
+    rng = np.random.default_rng(5)
+    n = moved.num_bodies
+    lfa = moved.acceleration + np.stack([rng.uniform(-3, 3, n), np.zeros(n), rng.uniform(-3, 3, n)], axis=1)
+    ref = OracleBatch(moved, form=form, last_frame_acceleration=lfa)
+    ref.narrowphase()
+    c = ref.contacts(0)
+    c["friction"] = np.full(len(c["penetration"]), 0.9)
+    c["restitution"] = np.full(len(c["penetration"]), 0.1)
+    extra = {"last_frame_acceleration": lfa, "inverse_inertia_world": st["iit_world"]}
+    return moved, c, extra, ref
+
+
 @pytest.mark.parametrize("form", [0, 1])
 def test_resolve_contacts_with_frame_inputs(form, cuda_lib):
     """last_frame_acceleration (the restitution and local-velocity terms of
-    contact.go:87-112,159-182) and an explicit world inverse inertia, as a
-    frame loop passes them after Integrate: the oracle that integrated the
-    frame against the entry point given that frame's values."""
-    sc = scenes.mixed(num_worlds=1, seed=32, min_bodies=24, max_bodies=24)
-    ref, moved, st = frame_state(sc, 150, form)
-    ref.narrowphase()
-    c = ref.contacts(0)
+    contact.go:87-112,159-182) and an explicit world inverse inertia against
+    the oracle given the same values."""
+    moved, c, extra, ref = frame_inputs(form)
     n = len(c["penetration"])
-    c["friction"] = np.full(n, 0.9)
-    c["restitution"] = np.full(n, 0.1)
-    # Integrate sets lastFrameAccelleration = Acceleration + forceAccum * inverseMass
-    # (rigidbody.go:222-223) with no force applied
-    extra = {"last_frame_acceleration": moved.acceleration, "inverse_inertia_world": st["iit_world"]}
-    stt, arrays, arr, ref = resolve_both(moved, c, 4 * n, form, ref=ref, extra=extra)
-    assert stt == 0, cuda_lib.cz_last_error()
+    st, arrays, arr, ref = resolve_both(moved, c, 4 * n, form, ref=ref, extra=extra)
+    assert st == 0, cuda_lib.cz_last_error()
     assert ref.stats()["vel_iterations"][0] > 0
     assert_matches_oracle(arrays, arr, ref)
     # the accelerations matter: without them the result differs
-    st0, arrays0, _, _ = resolve_both(moved, c, 4 * n, form, ref=OracleBatch(moved, form=form))
+    st0, arrays0, _, _ = resolve_both(moved, c, 4 * n, form)
+    assert st0 == 0
     assert not np.array_equal(arrays0["velocity"], arrays["velocity"])
 
 

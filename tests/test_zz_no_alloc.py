@@ -16,7 +16,7 @@ import numpy as np
 import pytest
 
 from cubez_gb300 import scenes
-from tests.test_gpu_api import (assert_matches_oracle, cz_contacts, frame_state, host_arrays, resolve_both,
+from tests.test_gpu_api import (assert_matches_oracle, cz_contacts, frame_inputs, host_arrays, resolve_both,
                                 scene_with_contacts)
 
 pytestmark = pytest.mark.gpu
@@ -95,16 +95,10 @@ def test_static_scratch_matches_existing_entry_point_twice(form, cuda_lib):
 @pytest.mark.parametrize("form", [0, 1])
 def test_static_scratch_with_frame_inputs(form, cuda_lib):
     """The optional inputs a frame loop passes after Integrate: last-frame
-    accelerations and the world inverse inertia, against the oracle that
-    integrated that frame and against the allocating entry point."""
-    sc = scenes.mixed(num_worlds=1, seed=32, min_bodies=24, max_bodies=24)
-    ref, moved, st = frame_state(sc, 150, form)
-    ref.narrowphase()
-    c = ref.contacts(0)
+    accelerations and the world inverse inertia, against the oracle given the
+    same values and against the allocating entry point."""
+    moved, c, extra, ref = frame_inputs(form)
     n = len(c["penetration"])
-    c["friction"] = np.full(n, 0.9)
-    c["restitution"] = np.full(n, 0.1)
-    extra = {"last_frame_acceleration": moved.acceleration, "inverse_inertia_world": st["iit_world"]}
     st_a, host, arr_a, ref = resolve_both(moved, c, 4 * n, form, ref=ref, extra=extra)
     assert st_a == 0, cuda_lib.cz_last_error()
     assert ref.stats()["vel_iterations"][0] > 0
