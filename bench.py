@@ -363,8 +363,8 @@ def run_ours(args):
                    "parallelism": "weak: %d worlds per GPU" % args.worlds},
         "fp32_plain": block("fp32"),
         "fp64": block("fp64"),
-        "mlp_over_fp64": (r32["value"] / fp64v) if fp64v else None,
-        "fp32_plain_over_fp64": (results["fp32"]["value"] / fp64v) if fp64v else None,
+        "mlp_over_fp64": (r32["value"] / fp64v) if fp64v and head == "fp32_mlp" else None,
+        "fp32_plain_over_fp64": (results["fp32"]["value"] / fp64v) if fp64v and "fp32" in results else None,
         "mlp_over_fp32_plain": (r32["value"] / results["fp32"]["value"]) if "fp32" in results else None,
         "warm_start": None if train_info is None else {"training": train_info,
                        "policy": "worlds whose previous solve used at most 1/%d of the iteration budget are "
@@ -458,7 +458,11 @@ def run_reference(args):
         return
     from cubez_gb300 import scenes
     from oracle.oracle import OracleBatch, hardware_threads
-    scene = scenes.precision(num_worlds=args.worlds, bodies=args.bodies, seed=3)
+    batched = args.workload == "batched"
+    if batched:
+        scene = scenes.mixed(num_worlds=args.worlds if args.worlds != 16384 else 4096, seed=2)
+    else:
+        scene = scenes.precision(num_worlds=args.worlds, bodies=args.bodies, seed=3)
     cores = os.cpu_count() or hardware_threads()
     nw = min(args.cpu_worlds, scene.num_worlds)
     sub = scene.subset(range(nw))
@@ -473,15 +477,18 @@ def run_reference(args):
     ms = total / args.steps * 1e3
     value = sub.num_bodies * args.frames / (ms / 1e3)
     line = {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "metric": "body-steps/s (batched float64, secondary)" if batched else METRIC, "value": value, "unit": UNIT,
+        "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded scenes)", "impl": "reference",
-        "config": {"workload": "precision: %d worlds x %d bodies, %d-frame rollout, dt=1/60; each step a sample of "
-                               "%d worlds" % (args.worlds, args.bodies, args.frames, nw),
+        "config": {"workload": ("batched: %d worlds x U{8..64} spheres/cubes, %d-frame rollout, dt=1/60, float64; "
+                                "each step a sample of %d worlds" % (scene.num_worlds, args.frames, nw)) if batched else
+                               ("precision: %d worlds x %d bodies, %d-frame rollout, dt=1/60; each step a sample of "
+                                "%d worlds" % (args.worlds, args.bodies, args.frames, nw)),
                    "parallelism": "host cores, one thread per world"},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
                          "sample": "%d of %d worlds x %d frames per step (the Go reference cannot be built here; "
-                                   "its float64 path restated in C++)" % (nw, args.worlds, args.frames)},
+                                   "its float64 path restated in C++)" % (nw, scene.num_worlds, args.frames)},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
@@ -554,6 +561,116 @@ def run_piles(args):
     print(json.dumps(line))
 
 
+def run_batched(args):
+    """The batched configuration: 4096 worlds of U{8..64} spheres and cubes in
+    the plain float64 form (bit-exact with the reference's arithmetic), one
+    600-frame rollout per step captured as one CUDA graph, restarted from the
+    same device-resident state; e2e through the C ABI with host buffers; the
+    oracle on the host's cores beside it."""
+    import torch
+    ws, rank, local = _dist()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    from cubez_gb300 import _lib, scenes
+    from cubez_gb300.batch import FORM_FP64, WorldBatch
+    nw = args.worlds if args.worlds != 16384 else 4096
+    frames = args.frames
+    scene = scenes.mixed(num_worlds=nw, seed=2 + 1000 * rank)
+    nb = scene.num_bodies
+    b = WorldBatch.from_scene(scene, form=FORM_FP64, device=local)
+    fixed = json.loads(args.tuning) if args.tuning else None
+    if fixed:
+        b.set_tuning(**fixed)
+    b.prepare_rollout(frames, DT)
+    b.snapshot()
+
+    def barrier():
+        if ws > 1:
+            import torch.distributed as dist
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    for _ in range(args.warmup):
+        b.restore()
+        b.step_timed(frames, DT)
+    b.counters(reset=True)
+    launches0 = _lib.kernel_launches()
+    tot, ph = 0.0, np.zeros(3)
+    clocks = Clocks(local)
+    with clocks:
+        for _ in range(args.steps):
+            b.restore()
+            _flush_l2()
+            barrier()
+            t, p = b.step_timed(frames, DT)
+            barrier()
+            tot += t
+            ph += p
+    launches = _lib.kernel_launches() - launches0
+    cnt = b.counters()
+    ms = tot / args.steps
+    if ws > 1:
+        import torch.distributed as dist
+        tt = torch.tensor([ms], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        ms = float(tt.item())
+    # e2e: upload from pinned host memory, the rollout, download
+    e2e = None
+    if not args.no_e2e:
+        pinned = {}
+        for k in scene.FIELDS:
+            v = np.ascontiguousarray(getattr(scene, k))
+            t = torch.empty(v.nbytes, dtype=torch.uint8, pin_memory=True)
+            a = np.frombuffer(t.numpy().data, dtype=v.dtype, count=v.size).reshape(v.shape)
+            a[...] = v
+            pinned[k] = (t, a)
+        arrays = {k: a for k, (t, a) in pinned.items()}
+        b.upload(**arrays)
+        b.step(frames, DT)
+        b.download()
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            b.upload(**arrays)
+            b.step(frames, DT)
+            b.download()
+        barrier()
+        e2e_s = (time.perf_counter() - t0) / args.steps
+        h2d = 43 * 8 * nb + 2 * nb + 4 * nb + 2 * 8 * int(b.info()["padded_bodies"])
+        d2h = 43 * 8 * nb + 2 * nb + 4 * nb + 4
+        e2e = {"value": nb * frames * ws / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+               "ms_per_step": e2e_s * 1e3}
+    info = b.info()
+    b.close()
+    if rank != 0:
+        return
+    cpu = None
+    if not args.no_cpu_baseline:
+        from oracle.oracle import OracleBatch, hardware_threads
+        cores = os.cpu_count() or hardware_threads()
+        sub = scene.subset(range(min(args.cpu_worlds, nw)))
+        ob = OracleBatch(sub)
+        t0 = time.perf_counter()
+        ob.step(frames, DT, 4, cores)
+        el = time.perf_counter() - t0
+        cpu = {"value": sub.num_bodies * frames / el, "unit": UNIT, "cores": cores, "kind": "port",
+               "sample": "%d of %d worlds x %d frames (float64 oracle, %.1f s)" % (sub.num_worlds, nw, frames, el)}
+    per = {k: v / (frames * args.steps) for k, v in cnt.items()}
+    line = {"metric": "body-steps/s (batched float64, secondary)", "value": nb * frames * ws / (ms / 1e3),
+            "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded scenes)",
+            "config": {"workload": "batched: %d worlds x U{8..64} spheres/cubes (%d bodies), %d-frame rollout, "
+                                   "dt=1/60, float64" % (nw, nb, frames), "step": "one %d-frame rollout" % frames,
+                       "l2": "explicit 252 MB flush before every timed rollout"},
+            "world_steps_per_s": nw * frames * ws / (ms / 1e3), "phase_ms": (ph / args.steps).tolist(),
+            "counters_per_frame": per, "gpu_launches": launches, "clocks": clocks.summary(), "e2e": e2e,
+            "batch": info, "cpu_baseline": cpu}
+    print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -565,7 +682,7 @@ def main():
     ap.add_argument("--frames", type=int, default=600)
     ap.add_argument("--cpu-worlds", type=int, default=2048)
     ap.add_argument("--train-worlds", type=int, default=4096)
-    ap.add_argument("--workload", default="precision", choices=["precision", "piles"])
+    ap.add_argument("--workload", default="precision", choices=["precision", "piles", "batched"])
     ap.add_argument("--fp64-steps", type=int, default=1)
     ap.add_argument("--fp64-warmup", type=int, default=1)
     ap.add_argument("--fp32-only", action="store_true")
@@ -581,6 +698,8 @@ def main():
     args.warmup_given = any(a.startswith("--warmup") for a in _sys.argv[1:])
     if args.workload == "piles" and args.impl != "reference":
         run_piles(args)
+    elif args.workload == "batched" and args.impl != "reference":
+        run_batched(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

@@ -45,7 +45,8 @@ class Contact(C.Structure):
 class Tuning(C.Structure):
     _fields_ = [("narrowphase_threads", C.c_int32), ("resolver_contacts", C.c_int32),
                 ("resolver_ctas_per_sm", C.c_int32), ("integrate_threads", C.c_int32), ("resolver_lanes", C.c_int32),
-                ("warm_start_budget_shift", C.c_int32), ("large_world_lanes", C.c_int32)]
+                ("warm_start_budget_shift", C.c_int32), ("large_world_lanes", C.c_int32),
+                ("broadphase_min_bodies", C.c_int32)]
 
 
 # every symbol include/cubez_gpu.h declares, with (restype, argtypes)
@@ -85,6 +86,7 @@ SIGNATURES = {
     "cz_batch_info": (C.c_int, [C.c_void_p, C.c_void_p]),
     "cz_counters": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32]),
     "cz_collide": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_int32]),
+    "cz_set_wait_test": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
     "cz_status_string": (C.c_char_p, [C.c_int]),
     "cz_last_error": (C.c_char_p, []),
     "cz_kernel_launches": (C.c_int64, []),

@@ -127,6 +127,9 @@ struct cz_batch {
   int np_threads = 128, np_grid = 1, rs_cs = 128, rs_grid = 1, rs_ctas_per_sm = 0, int_threads = 256;
   int rs_lanes = 8;  // lanes per world in the resolver (32 / rs_lanes worlds per warp)
   int big_lanes = 32; // lanes per world in the large-world resolver (16: two worlds per warp)
+  int wait_limit = 1 << 22;  // polls of the narrowphase's bounded wait
+  int wait_extra_tx = 0;     // test hook: bytes that wait expects beyond its copies
+  int grid_min_bodies = 128; // narrowphase grid for worlds of at least this many bodies (0: never)
   int mode = 0;      // resolver mode: 0 plain, 1 harvest, 2 learned warm start
   cz::MlpDev mlp{};  // device copy of the warm-start network
   void* mlp_mem = nullptr;
@@ -211,6 +214,9 @@ struct cz_batch {
     v.big_off = big_off;
     v.big_cnt = big_cnt;
     v.big_adj = big_adj;
+    v.wait_limit = wait_limit;
+    v.wait_extra_tx = wait_extra_tx;
+    v.grid_min_bodies = grid_min_bodies;
     return v;
   }
 };
@@ -598,8 +604,8 @@ int cz_set_tuning(cz_batch* b, const cz_tuning* t) {
   if (!b || !t) return fail(CZ_ERR_BAD_ARG, "cz_set_tuning: null argument");
   CZ_CUDA(cudaSetDevice(b->device));
   if (t->narrowphase_threads > 0) {
-    if (t->narrowphase_threads % 32 != 0 || t->narrowphase_threads > 1024)
-      return fail(CZ_ERR_BAD_ARG, "narrowphase_threads must be a multiple of 32, at most 1024");
+    if (t->narrowphase_threads % 32 != 0 || t->narrowphase_threads > 256)
+      return fail(CZ_ERR_BAD_ARG, "narrowphase_threads must be a multiple of 32, at most 256");
     b->np_threads = t->narrowphase_threads;
   }
   if (t->resolver_contacts > 0) b->rs_cs = (int)round_up(t->resolver_contacts, 32);
@@ -623,7 +629,19 @@ int cz_set_tuning(cz_batch* b, const cz_tuning* t) {
     if (t->warm_start_budget_shift > 8) return fail(CZ_ERR_BAD_ARG, "warm_start_budget_shift must be 1 to 8");
     b->warm_shift = t->warm_start_budget_shift;
   }
+  if (t->broadphase_min_bodies != 0) {
+    if (t->broadphase_min_bodies < -1) return fail(CZ_ERR_BAD_ARG, "broadphase_min_bodies must be -1 or positive");
+    b->grid_min_bodies = t->broadphase_min_bodies < 0 ? 0 : t->broadphase_min_bodies;
+  }
   return configure(b);
+}
+
+int cz_set_wait_test(cz_batch* b, int32_t extra_bytes, int32_t wait_limit) {
+  if (!b || extra_bytes < 0 || extra_bytes > 4096 || wait_limit < 0) return CZ_ERR_BAD_ARG;
+  b->wait_extra_tx = extra_bytes;
+  b->wait_limit = wait_limit > 0 ? wait_limit : (1 << 22);
+  drop_graphs(b);
+  return CZ_OK;
 }
 
 int cz_get_tuning(cz_batch* b, cz_tuning* t) {
@@ -634,6 +652,7 @@ int cz_get_tuning(cz_batch* b, cz_tuning* t) {
   t->integrate_threads = b->int_threads;
   t->resolver_lanes = b->rs_lanes;
   t->warm_start_budget_shift = b->warm_shift;
+  t->broadphase_min_bodies = b->grid_min_bodies > 0 ? b->grid_min_bodies : -1;
   t->large_world_lanes = b->big_lanes;
   return CZ_OK;
 }

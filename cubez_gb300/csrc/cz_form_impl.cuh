@@ -68,6 +68,9 @@ static BatchView<R> view_of(const HostView& h) {
   v.big_off = h.big_off;
   v.big_cnt = h.big_cnt;
   v.big_adj = h.big_adj;
+  v.wait_limit = h.wait_limit;
+  v.wait_extra_tx = h.wait_extra_tx;
+  v.grid_min_bodies = h.grid_min_bodies;
   return v;
 }
 

@@ -67,6 +67,9 @@ struct HostView {
   int* big_off;
   int* big_cnt;
   int* big_adj;
+  int wait_limit;
+  int wait_extra_tx;
+  int grid_min_bodies;
 };
 
 // Staging layout of host body data on the device (doubles, field blocks of n):

@@ -270,7 +270,10 @@ __device__ int cube_sphere(const xf<R>& tc, const v3<R>& h, int ic, const xf<R>&
   v3<R> cw = xf_mul(tc, V<R>(cl[0], cl[1], cl[2]));
   v3<R> nrm = cw;
   sub(nrm, pos);
-  if (real_equal<R>(mag(nrm), (R)0)) {
+  // colliders.go:417-421; the precision form also takes the fallback when the
+  // centre needed no clamping (float32 rounding of the round trip exceeds the
+  // reference's absolute 1e-14)
+  if (real_equal<R>(mag(nrm), (R)0) || (sizeof(R) < sizeof(double) && dist == (R)0)) {
     nrm = V<R>(svel_rows[0], svel_rows[svel_stride], svel_rows[2 * svel_stride]);
   }
   normalize(nrm);
@@ -410,31 +413,53 @@ struct Cull {
   }
 };
 
-// One ordered pair (i, j): CheckForCollisions(collider i, collider j)
-// (colliders.go:718-747 with the forwarding of colliders.go:209-213).
-template <class R>
-__device__ int pair_test(const NPTile<R>& tl, int i, int j, const BatchView<R>& v, int bstart, NPContact<R>& c,
-                         uint32_t& err) {
+// Whether the float32 culls rule out any contact of the ordered pair (i, j).
+template <class R> __device__ __forceinline__ bool pair_culled(const NPTile<R>& tl, int i, int j) {
   const int si = tl.shape[i], sj = tl.shape[j];
   const Cull cl{tl.cull, tl.nbs};
+  if (sj == 0) return si == 0 ? cl.spheres(i, j) : cl.box_sphere(i, j);
+  return si == 0 ? cl.box_sphere(j, i) : cl.boxes(i, j);
+}
+
+// One ordered pair (i, j) past the culls: CheckForCollisions(collider i,
+// collider j) (colliders.go:718-747 with the forwarding of colliders.go:209-213).
+template <class R>
+__device__ int pair_full(const NPTile<R>& tl, int i, int j, const BatchView<R>& v, int bstart, NPContact<R>& c,
+                         uint32_t& err) {
+  const int si = tl.shape[i], sj = tl.shape[j];
   if (sj == 0) {
-    if (si == 0) {
-      if (cl.spheres(i, j)) return 0;
+    if (si == 0)
       return sphere_sphere(V<R>(tl.T[9 * tl.nbs + i], tl.T[10 * tl.nbs + i], tl.T[11 * tl.nbs + i]), tl.radius(i), i,
                            V<R>(tl.T[9 * tl.nbs + j], tl.T[10 * tl.nbs + j], tl.T[11 * tl.nbs + j]), tl.radius(j), j,
                            c);
-    }
-    if (cl.box_sphere(i, j)) return 0;
     return cube_sphere(tl.xform(i), tl.half(i), i, tl.xform(j), tl.radius(j), j,
                        v.body + (long long)B_VX * v.nb_pad + bstart + j, v.nb_pad, c);
   }
-  if (si == 0) {
-    if (cl.box_sphere(j, i)) return 0;
+  if (si == 0)
     return cube_sphere(tl.xform(j), tl.half(j), j, tl.xform(i), tl.radius(i), i,
                        v.body + (long long)B_VX * v.nb_pad + bstart + i, v.nb_pad, c);
-  }
-  if (cl.boxes(i, j)) return 0;
   return cube_cube(tl.xform(i), tl.half(i), i, tl.xform(j), tl.half(j), j, c, err);
+}
+
+template <class R>
+__device__ __forceinline__ int pair_test(const NPTile<R>& tl, int i, int j, const BatchView<R>& v, int bstart,
+                                         NPContact<R>& c, uint32_t& err) {
+  return pair_culled(tl, i, j) ? 0 : pair_full(tl, i, j, v, bstart, c, err);
+}
+
+// Whether a float32 cull rules out any contact of body i with the half-space
+// n.x <= offset: a sphere's d = n.c - r (colliders.go:190-192), a cube's
+// n.c - (projected half-size) with the projection at most |n| |h|_2
+// (colliders.go:750-770); the margin is the pair culls' (1 mm + 1e-5 of the
+// magnitudes).  A cube with a non-rigid Offset has an infinite radius.
+template <class R> __device__ __forceinline__ bool plane_culled(const NPTile<R>& tl, int i, const BatchView<R>& v) {
+  const float nx = (float)v.plane_nx, ny = (float)v.plane_ny, nz = (float)v.plane_nz, off = (float)v.plane_offset;
+  const float cx = tl.cull[i], cy = tl.cull[tl.nbs + i], cz = tl.cull[2 * tl.nbs + i];
+  const float d = nx * cx + ny * cy + nz * cz;
+  const float nlen = sqrtf(nx * nx + ny * ny + nz * nz) * 1.0001f;
+  const float r = tl.shape[i] == 0 ? tl.cull[3 * tl.nbs + i] : tl.cull[3 * tl.nbs + i] * nlen;
+  const float scale = 1.f + (fabsf(cx) + fabsf(cy) + fabsf(cz)) * nlen + fabsf(off);
+  return d - r > off + 1e-3f + 1e-5f * scale;  // false for NaN and infinite radii
 }
 
 // ---- bulk async copy (TMA engine) helpers
@@ -470,12 +495,19 @@ __device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned pari
   return false;
 }
 
+// Units past the culls held for their full tests: at least twice the largest
+// CTA (256), and at least one body's units (the grid path lists a body's
+// units together).
+constexpr int kSurvivors = 512;
+__host__ __device__ inline int np_surv_cap(int nbs) { return nbs + 1 > kSurvivors ? ((nbs + 32) & ~31) : kSurvivors; }
+
 template <class R> __host__ __device__ inline size_t np_smem_bytes(int nbs) {
   size_t b = 16;                                  // mbarrier + pad
   b += (size_t)(11 + 12) * nbs * sizeof(R);       // staged rows + transforms
   b += (size_t)nbs * sizeof(int);                 // shape
   b += (size_t)5 * nbs * sizeof(float);           // cull data
-  b += 2 * 33 * sizeof(int);                      // scan scratch (double-buffered) + world id
+  b += 2 * 33 * sizeof(int);                      // scan scratch (double-buffered) + world id + wait outcome
+  b += (size_t)np_surv_cap(nbs) * sizeof(int);    // units past the culls, awaiting their full tests
   return b;
 }
 
@@ -588,6 +620,216 @@ __device__ __forceinline__ void np_emit(const NPTile<R>& tl, const BatchView<R>&
   }
 }
 
+// The full tests of the listed units (unit u = i * n + k: k = 0 the
+// half-space, else the pair with j = k - 1, skipping i), in list order and in
+// chunks of the CTA's size, emitting their contacts at out onwards.
+template <class R>
+__device__ void np_flush(const NPTile<R>& tl, const BatchView<R>& v, int bstart, int n, long long cs, int cap,
+                         const int* surv, int nsurv, int* scan, int& parity, int& out, uint32_t& err) {
+  for (int sb = 0; sb < nsurv; sb += blockDim.x) {
+    const int si = sb + threadIdx.x;
+    int cnt = 0, i = 0, k = 0;
+    NPContact<R> c;
+    if (si < nsurv) {
+      const int uu = surv[si];
+      i = uu / n;
+      k = uu - i * n;
+      if (k == 0) {
+        cnt = plane_contacts<R>(tl, i, v, nullptr, nullptr, 0, 0);
+      } else {
+        int j = k - 1;
+        if (j >= i) ++j;
+        cnt = pair_full<R>(tl, i, j, v, bstart, c, err);
+      }
+    }
+    int excl, total;
+    np_chunk_scan(cnt, scan, parity, &excl, &total);
+    parity ^= 1;
+    np_emit<R>(tl, v, cs, cap, out + excl, cnt, i, k == 0, c);
+    out += total;
+  }
+}
+
+// ---- broadphase: a uniform grid over a large world's bodies
+//
+// A pair (i, j) passes the float32 culls only if its centres are within
+// reach_i + reach_j + 1 mm + 1e-5 (1 + |c_i|_1 + |c_j|_1), with reach = the
+// larger of 1.1 |h|_2 and |h|_1 for a box, 3 r for a sphere (the thresholds
+// of Cull).  With cells at least that wide for every pair of the world, the
+// pairs the culls keep are all between neighbouring cells: the grid drops
+// only pairs the culls reject.  Each body's kept units are listed in
+// ascending unit order and bodies in index order, so the contact list is the
+// all-pairs path's, bit for bit.
+
+// Grid scratch inside the staged position / orientation rows, which are
+// dead once the collider transforms are built.
+struct NPGrid {
+  float* red;   // [8 warps][8] block reductions
+  int* info;    // [8]: ok, gx, gy, gz, ncells, last list length
+  float* finfo; // [4]: origin xyz, cell size
+  int* cell;    // [cells_cap + 1] counts, then cursor / end of each cell
+  int* sorted;  // [n] bodies ordered by cell
+  int* cellof;  // [n] linear cell of each body
+  int cells_cap;
+};
+
+template <class R> __device__ __forceinline__ NPGrid np_grid_scratch(const NPTile<R>& tl) {
+  NPGrid g;
+  unsigned char* base = reinterpret_cast<unsigned char*>(tl.stage);
+  const int words = (int)((size_t)7 * tl.nbs * sizeof(R) / 4);
+  g.red = reinterpret_cast<float*>(base);
+  g.info = reinterpret_cast<int*>(base) + 64;
+  g.finfo = reinterpret_cast<float*>(g.info + 8);
+  g.sorted = g.info + 12;
+  g.cellof = g.sorted + tl.nbs;
+  g.cell = g.cellof + tl.nbs;
+  g.cells_cap = words - 76 - 2 * tl.nbs - 1;
+  return g;
+}
+
+// Block-wide max of 8 floats (NaN in any input gives NaN through the
+// comparison trick below: a value that is not >= itself is kept).
+__device__ __forceinline__ void np_block_max8(float (&x)[8], float* red) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+  for (int q = 0; q < 8; ++q)
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) {
+      const float y = __shfl_xor_sync(FULL, x[q], d);
+      x[q] = (y > x[q] || y != y) ? y : x[q];
+    }
+  if (lane == 0)
+#pragma unroll
+    for (int q = 0; q < 8; ++q) red[wid * 8 + q] = x[q];
+  __syncthreads();
+#pragma unroll
+  for (int q = 0; q < 8; ++q) {
+    float m = red[q];
+    for (int k = 1; k < nw; ++k) {
+      const float y = red[k * 8 + q];
+      m = (y > m || y != y) ? y : m;
+    }
+    x[q] = m;
+  }
+  __syncthreads();
+}
+
+// Builds the grid of one world; false (uniform over the CTA) when it would
+// not help or cannot be sized: non-finite centres or radii (a non-rigid
+// Offset's infinite radius included), or more cells than the scratch holds.
+template <class R> __device__ bool np_grid_build(const NPTile<R>& tl, int n, const NPGrid& g, int* scan, int& parity) {
+  const int nbs = tl.nbs;
+  float x[8];
+#pragma unroll
+  for (int q = 0; q < 8; ++q) x[q] = -__int_as_float(0x7f800000);
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const float cx = tl.cull[i], cy = tl.cull[nbs + i], cz = tl.cull[2 * nbs + i];
+    const float rb = tl.cull[3 * nbs + i], rl = tl.cull[4 * nbs + i];
+    const float reach = tl.shape[i] == 0 ? 3.f * rb : fmaxf(1.1f * rb, rl);
+    const float fin = (isfinite(cx) && isfinite(cy) && isfinite(cz) && isfinite(reach)) ? 0.f : 1.f;
+    // max of: the centres (the box's upper corner), their negations (the
+    // lower corner), the reach, non-finite flag
+    const float v8[8] = {cx, cy, cz, -cx, -cy, -cz, reach, fin};
+#pragma unroll
+    for (int q = 0; q < 8; ++q) x[q] = (v8[q] > x[q] || v8[q] != v8[q]) ? v8[q] : x[q];
+  }
+  np_block_max8(x, g.red);
+  if (threadIdx.x == 0) {
+    int ok = x[7] == 0.f && x[6] == x[6];
+    // |c|_1 of every centre is at most the larger corner's per axis
+    const float m1 = fmaxf(fabsf(x[0]), fabsf(x[3])) + fmaxf(fabsf(x[1]), fabsf(x[4])) +
+                     fmaxf(fabsf(x[2]), fabsf(x[5]));
+    // cell size: every kept pair is within 2 * max reach + the culls' margin
+    const float L = (2.f * x[6] + 1e-3f + 1e-5f * (1.f + 2.f * m1)) * 1.001f + 1e-6f;
+    const float ox = -x[3], oy = -x[4], oz = -x[5];
+    int gx = 0, gy = 0, gz = 0;
+    if (ok && L > 0.f) {
+      const float ex = (x[0] - ox) / L, ey = (x[1] - oy) / L, ez = (x[2] - oz) / L;
+      ok = ex < 1e6f && ey < 1e6f && ez < 1e6f;
+      if (ok) {
+        gx = (int)ex + 1;
+        gy = (int)ey + 1;
+        gz = (int)ez + 1;
+        ok = (long long)gx * gy * gz <= g.cells_cap;
+      }
+    } else {
+      ok = 0;
+    }
+    g.info[0] = ok;
+    g.info[1] = gx;
+    g.info[2] = gy;
+    g.info[3] = gz;
+    g.info[4] = gx * gy * gz;
+    g.finfo[0] = ox;
+    g.finfo[1] = oy;
+    g.finfo[2] = oz;
+    g.finfo[3] = L;
+  }
+  __syncthreads();
+  if (!g.info[0]) return false;
+  const int gx = g.info[1], gy = g.info[2], gz = g.info[3], nc = g.info[4];
+  const float ox = g.finfo[0], oy = g.finfo[1], oz = g.finfo[2], L = g.finfo[3];
+  for (int c = threadIdx.x; c <= nc; c += blockDim.x) g.cell[c] = 0;
+  __syncthreads();
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const int cx = min((int)((tl.cull[i] - ox) / L), gx - 1);
+    const int cy = min((int)((tl.cull[nbs + i] - oy) / L), gy - 1);
+    const int cz = min((int)((tl.cull[2 * nbs + i] - oz) / L), gz - 1);
+    const int c = (cz * gy + cy) * gx + cx;
+    g.cellof[i] = c;
+    atomicAdd(&g.cell[c], 1);
+  }
+  __syncthreads();
+  // exclusive scan of the counts: cell[c] = first slot of cell c
+  int run = 0;
+  for (int b0 = 0; b0 < nc; b0 += blockDim.x) {
+    const int c = b0 + threadIdx.x;
+    const int cnt = c < nc ? g.cell[c] : 0;
+    int excl, total;
+    np_chunk_scan(cnt, scan, parity, &excl, &total);
+    parity ^= 1;
+    if (c < nc) g.cell[c] = run + excl;
+    run += total;
+  }
+  __syncthreads();
+  // scatter; afterwards cell[c] is the end of cell c (the start of c + 1)
+  for (int i = threadIdx.x; i < n; i += blockDim.x) g.sorted[atomicAdd(&g.cell[g.cellof[i]], 1)] = i;
+  __syncthreads();
+  return true;
+}
+
+// Body i's units past the culls from its 27 neighbouring cells: counted, or
+// written at dst (plane unit, then the pairs, unsorted).
+template <class R>
+__device__ int np_grid_units(const NPTile<R>& tl, const BatchView<R>& v, const NPGrid& g, int n, int i, int* dst) {
+  int cnt = 0;
+  if (!plane_culled(tl, i, v)) {
+    if (dst) dst[cnt] = i * n;
+    ++cnt;
+  }
+  const int gx = g.info[1], gy = g.info[2], gz = g.info[3];
+  const int c = g.cellof[i];
+  const int cx = c % gx, cy = (c / gx) % gy, cz = c / (gx * gy);
+  for (int dz = -1; dz <= 1; ++dz) {
+    if (cz + dz < 0 || cz + dz >= gz) continue;
+    for (int dy = -1; dy <= 1; ++dy) {
+      if (cy + dy < 0 || cy + dy >= gy) continue;
+      for (int dx = -1; dx <= 1; ++dx) {
+        if (cx + dx < 0 || cx + dx >= gx) continue;
+        const int nc = ((cz + dz) * gy + cy + dy) * gx + cx + dx;
+        const int s0 = nc == 0 ? 0 : g.cell[nc - 1], s1 = g.cell[nc];
+        for (int s = s0; s < s1; ++s) {
+          const int j = g.sorted[s];
+          if (j == i || pair_culled(tl, i, j)) continue;
+          if (dst) dst[cnt] = i * n + (j < i ? j + 1 : j);
+          ++cnt;
+        }
+      }
+    }
+  }
+  return cnt;
+}
+
 template <class R>
 __global__ void __launch_bounds__(256) k_narrowphase(BatchView<R> v, int nbs) {
   extern __shared__ __align__(128) unsigned char smem[];
@@ -598,7 +840,8 @@ __global__ void __launch_bounds__(256) k_narrowphase(BatchView<R> v, int nbs) {
   tl.T = tl.stage + 11 * nbs;
   tl.shape = reinterpret_cast<int*>(tl.T + 12 * nbs);
   tl.cull = reinterpret_cast<float*>(tl.shape + nbs);
-  int* scan = reinterpret_cast<int*>(tl.cull + 5 * nbs);  // [2][32] + [64] world id
+  int* scan = reinterpret_cast<int*>(tl.cull + 5 * nbs);  // [2][32] + [64] world id + [65] wait outcome
+  int* surv = scan + 66;                                   // [kSurvivors] units past the culls
   const int tid = threadIdx.x;
   if (tid == 0) mbar_init(bar, 1);
   __syncthreads();
@@ -628,49 +871,99 @@ __global__ void __launch_bounds__(256) k_narrowphase(BatchView<R> v, int nbs) {
       // order smem accesses of the previous world before the async-proxy writes
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       const unsigned rb = (unsigned)(n4 * sizeof(R));
-      mbar_expect_tx(bar, rb * 11u + (unsigned)(n4 * sizeof(int)));
+      mbar_expect_tx(bar, rb * 11u + (unsigned)(n4 * sizeof(int)) + (unsigned)v.wait_extra_tx);
 #pragma unroll 1
       for (int r = 0; r < 11; ++r) bulk_g2s(tl.stage + r * nbs, v.body + (long long)r * v.nb_pad + bstart, rb, bar);
       bulk_g2s(tl.shape, v.shape + bstart, (unsigned)(n4 * sizeof(int)), bar);
     }
     if (n4 > 0) {
-      bool ok = mbar_wait(bar, phase, 1 << 22);
-      phase ^= 1u;
-      if (!ok) {  // give up on the whole launch; the copies are bounded and tiny, so this is a fault signal
+      // Thread 0 waits, bounded, and decides for the CTA; the others then
+      // observe the completed phase themselves (their acquire of the copies).
+      if (tid == 0) scan[65] = mbar_wait(bar, phase, v.wait_limit) ? 1 : 0;
+      __syncthreads();
+      const bool ok = scan[65] != 0;
+      if (!ok) {
+        // Give up on this CTA's worlds (the copies are a few KB, so this
+        // signals a fault) and report it.  The copies issued may still be
+        // landing in this CTA's shared memory: one more bounded wait for
+        // them before the CTA ends.
         if (tid == 0) {
           v.world_status[w] |= ST_TIMEOUT;
           atomicOr(v.status, ST_TIMEOUT);
+          mbar_wait(bar, phase, v.wait_limit);
         }
+        __syncthreads();
         return;
       }
+      if (tid != 0) mbar_wait(bar, phase, v.wait_limit);
+      phase ^= 1u;
     }
     np_build_tile(tl, n, v.offset ? v.offset + bstart : nullptr, v.nb_pad);
     __syncthreads();
     const long long cs = v.contact_start[w];
     const int cap = v.contact_cap[w];
-    const long long U = (long long)n * n;
-    int out = 0;
+    const int U = n * n;  // ordered units: for body i, the half-space (k = 0), then k - 1 = j skipping i
+    const int scap = np_surv_cap(nbs);
+    int out = 0, nsurv = 0;
     uint32_t err = 0;
-    for (long long base = 0; base < U; base += blockDim.x) {
-      const long long u = base + tid;
-      int cnt = 0, i = 0, k = 0;
-      NPContact<R> c;
-      if (u < U) {
-        i = (int)(u / n);
-        k = (int)(u - (long long)i * n);
-        if (k == 0) {
-          cnt = plane_contacts<R>(tl, i, v, nullptr, nullptr, 0, 0);
-        } else {
+    const NPGrid g = np_grid_scratch(tl);
+    if (v.grid_min_bodies > 0 && n >= v.grid_min_bodies && np_grid_build(tl, n, g, scan, chunk_parity)) {
+      // Grid: each body's kept units (counted, then listed and sorted), as
+      // many bodies at a time as the list holds, then their full tests.
+      for (int ib = 0; ib < n;) {
+        const int i = ib + tid;
+        const int cnt = i < n ? np_grid_units(tl, v, g, n, i, nullptr) : 0;
+        int excl, total;
+        np_chunk_scan(cnt, scan, chunk_parity, &excl, &total);
+        chunk_parity ^= 1;
+        const bool fits = i < n && excl + cnt <= scap;  // a prefix of the bodies: at least body ib
+        const int m = __syncthreads_count(fits);
+        if (fits) {
+          int* d = surv + excl;
+          np_grid_units(tl, v, g, n, i, d);
+          for (int a = 1; a < cnt; ++a) {  // ascending unit order (the plane unit, k = 0, first)
+            const int key = d[a];
+            int b = a - 1;
+            while (b >= 0 && d[b] > key) {
+              d[b + 1] = d[b];
+              --b;
+            }
+            d[b + 1] = key;
+          }
+          if (tid == m - 1) g.info[5] = excl + cnt;
+        }
+        __syncthreads();
+        nsurv = g.info[5];
+        np_flush(tl, v, bstart, n, cs, cap, surv, nsurv, scan, chunk_parity, out, err);
+        __syncthreads();
+        ib += m;
+      }
+    } else {
+      // All pairs: the culls run over every unit; the units they keep are
+      // listed in unit order and get their full tests in chunks of the CTA's
+      // size, so the lanes of a warp run the costly tests together.
+      // Counting, scanning and emitting in list order keeps the reference's
+      // contact order.
+      for (int base = 0; base < U; base += blockDim.x) {
+        const int u = base + tid;
+        bool keep = false;
+        if (u < U) {
+          const int i = u / n, k = u - i * n;
           int j = k - 1;
           if (j >= i) ++j;
-          cnt = pair_test<R>(tl, i, j, v, bstart, c, err);
+          keep = k == 0 ? !plane_culled(tl, i, v) : !pair_culled(tl, i, j);
         }
+        int excl, total;
+        np_chunk_scan(keep ? 1 : 0, scan, chunk_parity, &excl, &total);
+        chunk_parity ^= 1;
+        if (keep) surv[nsurv + excl] = u;
+        nsurv += total;
+        if (nsurv <= scap - (int)blockDim.x && base + (int)blockDim.x < U) continue;
+        __syncthreads();
+        np_flush(tl, v, bstart, n, cs, cap, surv, nsurv, scan, chunk_parity, out, err);
+        nsurv = 0;
+        __syncthreads();
       }
-      int excl, total;
-      np_chunk_scan(cnt, scan, chunk_parity, &excl, &total);
-      chunk_parity ^= 1;
-      np_emit<R>(tl, v, cs, cap, out + excl, cnt, i, k == 0, c);
-      out += total;
     }
     if (err) {
       atomicOr(&v.world_status[w], err);

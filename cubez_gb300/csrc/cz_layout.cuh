@@ -110,7 +110,7 @@ template <class R> struct BatchView {
   R* contact;           // [C_NROWS][nc_total]
   int* contact_bodies;  // [nc_total]
   R* work;              // [W_NROWS][nc_total]
-  void* kmat;           // [9][nc_total] island type: K of each contact's friction solve
+  void* kmat;           // [9][nc_total] reals: K of each contact's friction solve (inverted in the island type)
   R* kdv;               // [3][nc_total]: the friction response's first row
   int* work_bodies;     // [nc_total]
   long long nc_total;
@@ -149,6 +149,12 @@ template <class R> struct BatchView {
   int* big_off;          // [nb_pad] start of each body's contact list in its world's segment
   int* big_cnt;          // [nb_pad] end of each body's contact list
   int* big_adj;          // [2 * nc_total] contact lists, a world's segment at 2 * contact_start
+  // the narrowphase's bounded wait on its staging copies: polls before it
+  // gives up, and extra bytes expected beyond those copied (0; a test raises
+  // it so that the wait runs out with every real copy landed)
+  int wait_limit;
+  int wait_extra_tx;
+  int grid_min_bodies;  // narrowphase: worlds of at least this many bodies use the grid (0: none)
 };
 
 }  // namespace cz

@@ -104,6 +104,18 @@ template <class R> __device__ __forceinline__ void add_scaled_vector(q4<R>& q, c
   q.y += t.y * (R)0.5;
   q.z += t.z * (R)0.5;
 }
+// AddScaledVector(v, 1) of an orientation held in the island type W
+// (applyPositionChange, contact.go:374-375): the increment 0.5 * (v q) in R
+// from q rounded to R, accumulated in W.  With R == W it is AddScaledVector.
+template <class R, class W> __device__ __forceinline__ void add_scaled_vector_island(q4<W>& q, const v3<R>& v) {
+  const q4<R> qr = cvtq<R>(q);
+  q4<R> t{(R)0, v.x * (R)1, v.y * (R)1, v.z * (R)1};
+  t = qmul(t, qr);
+  q.w += (W)(t.w * (R)0.5);
+  q.x += (W)(t.x * (R)0.5);
+  q.y += (W)(t.y * (R)0.5);
+  q.z += (W)(t.z * (R)0.5);
+}
 // quaternion.go:77-99
 template <class R> __device__ __forceinline__ void qnormalize(q4<R>& q) {
   R len = sqrt_<R>(q.w * q.w + q.x * q.x + q.y * q.y + q.z * q.z);

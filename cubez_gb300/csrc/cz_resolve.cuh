@@ -55,7 +55,7 @@ template <class R, class W> struct RCtx {
   long long wst;
   R* jw;          // impulse rows J0..J2 (row stride jst)
   long long jst;
-  W* kw;          // per contact: K of the friction solve, 9 rows (row stride kst)
+  R* kw;          // per contact: K of the friction solve (inverted in W, kept in R), 9 rows (row stride kst)
   R* kr;          // per contact: the response matrix's first row, 3 rows
   long long kst;
   const R* gmat;  // friction / restitution rows of the contact list (null: 0.9 / 0.1)
@@ -65,7 +65,7 @@ template <class R, class W> struct RCtx {
   __device__ __forceinline__ R& Bf(int r, int i) const { return br[r * nbs + i]; }
   __device__ __forceinline__ R& Cf(int f, int k) const { return cw[(long long)f * cst + k]; }
   __device__ __forceinline__ R& J(int c, int k) const { return jw[(long long)c * jst + k]; }
-  __device__ __forceinline__ W& K(int q, int k) const { return kw[(long long)q * kst + k]; }
+  __device__ __forceinline__ R& K(int q, int k) const { return kw[(long long)q * kst + k]; }
   __device__ __forceinline__ R& KD(int q, int k) const { return kr[(long long)q * kst + k]; }
   __device__ __forceinline__ int& WI(int r, int i) const { return wi[(long long)r * wst + i]; }
   __device__ __forceinline__ R& Save(int r, int i) const { return save[(long long)r * wst + i]; }
@@ -300,7 +300,7 @@ __device__ void apply_position_change(const RCtx<R, W>& x, const BatchView<R>& v
     x.P(1, b) += (W)(n.y * lm);
     x.P(2, b) += (W)(n.z * lm);
     q4<W> q{x.P(3, b), x.P(4, b), x.P(5, b), x.P(6, b)};
-    add_scaled_vector(q, cvt<W>(ang), (W)1);
+    add_scaled_vector_island<R, W>(q, ang);
     qnormalize(q);
     x.P(3, b) = q.w; x.P(4, b) = q.x; x.P(5, b) = q.y; x.P(6, b) = q.z;
     if (!x.aw[b]) {
@@ -350,7 +350,8 @@ __device__ __forceinline__ m3<R> friction_response(const RCtx<R, W>& x, int k, i
 
 // The matrices of contact k's friction solve for the whole of
 // adjustVelocities: K = Invert(response) in W (contact.go:577-580,
-// matrix.go:125-153) and the response's first row (R).  They depend on the
+// matrix.go:125-153), kept in R for the solve, and the response's first row
+// (R).  They depend on the
 // relative positions, the basis, the inverse masses and the bodies' world
 // inverse inertia, none of which adjustVelocities changes, so computing them
 // once, lane-parallel, at the start of the phase gives exactly the values the
@@ -365,21 +366,22 @@ template <class R, class W> __device__ __forceinline__ void friction_prepare(con
   for (int q = 0; q < 9; ++q) dv_w.m[q] = (W)dv.m[q];
   const m3<W> K = invert(dv_w);
 #pragma unroll
-  for (int q = 0; q < 9; ++q) x.K(q, k) = K.m[q];
+  for (int q = 0; q < 9; ++q) x.K(q, k) = (R)K.m[q];
   x.KD(0, k) = dv.m[0];
   x.KD(1, k) = dv.m[3];
   x.KD(2, k) = dv.m[6];
 }
 
 // calculateFrictionImpulse, contact.go:533-606, from the matrices of
-// friction_prepare: the solve in W, then the dynamic-friction correction.
+// friction_prepare: the solve K * (desired delta velocity, -vy, -vz) in R,
+// then the dynamic-friction correction.
 template <class R, class W> __device__ v3<R> friction_impulse(const RCtx<R, W>& x, int k) {
-  m3<W> K;
+  m3<R> K;
 #pragma unroll
   for (int q = 0; q < 9; ++q) K.m[q] = x.K(q, k);
   const R ddv = x.Cf(W_DDV, k);
-  const v3<W> kill = V<W>((W)ddv, (W)-x.Cf(W_CVY, k), (W)-x.Cf(W_CVZ, k));
-  v3<R> ic = cvt<R>(mulv(K, kill));
+  const v3<R> kill = V<R>(ddv, -x.Cf(W_CVY, k), -x.Cf(W_CVZ, k));
+  v3<R> ic = mulv(K, kill);
   const R fr = x.friction(k);
   R planar = sqrt_<R>(ic.y * ic.y + ic.z * ic.z);
   if (planar > ic.x * fr) {
@@ -527,7 +529,7 @@ __device__ __forceinline__ void bind_contacts(Slot<R, W>& s, const BatchView<R>&
   }
   x.gmat = v.uniform_material ? nullptr : v.contact + (long long)C_FRIC * v.nc_total + cst;
   x.gst = (long long)(C_REST - C_FRIC) * v.nc_total;
-  x.kw = reinterpret_cast<W*>(v.kmat) + cst;
+  x.kw = reinterpret_cast<R*>(v.kmat) + cst;
   x.kr = v.kdv + cst;
   x.kst = v.nc_total;
 }

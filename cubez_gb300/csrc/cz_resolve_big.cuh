@@ -125,7 +125,7 @@ __global__ void __launch_bounds__(32) k_resolve_big(BatchView<R> v, R dt) {
   x.save = x.delta = x.jw = nullptr;
   x.wi = nullptr;
   x.wst = x.jst = 0;
-  x.kw = reinterpret_cast<W*>(v.kmat) + cst;
+  x.kw = reinterpret_cast<R*>(v.kmat) + cst;
   x.kr = v.kdv + cst;
   x.kst = v.nc_total;
   const bool active = has && C > 0 && dt > (R)0;  // ResolveContacts guards, contact.go:210-212

@@ -235,6 +235,9 @@ cz::HostView static_view(unsigned char* scratch, int n) {
   v.contact_writeback = 1;
   v.uniform_material = 0;
   v.mode = 0;
+  v.wait_limit = 1 << 22;
+  v.wait_extra_tx = 0;
+  v.grid_min_bodies = 0;
   return v;
 }
 

@@ -272,9 +272,25 @@ typedef struct cz_tuning {
                                       (1 to 8; default 2) */
   int32_t large_world_lanes;   /* lanes per world of more than 64 bodies: 32 (the default) or
                                   16 (two worlds per warp in lockstep) */
+  int32_t broadphase_min_bodies; /* the narrowphase bins the bodies of worlds of at least this many
+                                    bodies in a uniform grid and tests only pairs of neighbouring
+                                    cells (default 128; -1 = never).  The grid drops only pairs the
+                                    float32 culls reject and keeps the reference's pair order, so
+                                    contact lists are the same bit for bit (an ordered all-pairs
+                                    loop, examples/cubedrop.go:41-67, that the reference marks as
+                                    O(n^2) at examples/cubedrop.go:54 and README.md:98-99) */
 } cz_tuning;
 int cz_set_tuning(cz_batch* batch, const cz_tuning* tuning);
 int cz_get_tuning(cz_batch* batch, cz_tuning* tuning);
+
+/* Test hook for the failure path of the narrowphase's one device wait (no
+ * counterpart in the reference).  The narrowphase stages each world's bodies
+ * with bulk copies and waits, bounded, for their bytes; with extra_bytes > 0
+ * it expects that many bytes more than it copies, so the wait runs out after
+ * wait_limit polls (0 = the default limit) with every real copy landed, and
+ * the call reports CZ_ERR_TIMEOUT.  cz_set_wait_test(batch, 0, 0) restores
+ * the normal wait; the batch then steps on as before. */
+int cz_set_wait_test(cz_batch* batch, int32_t extra_bytes, int32_t wait_limit);
 
 /* Error reporting. */
 const char* cz_status_string(int status);

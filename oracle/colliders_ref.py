@@ -146,7 +146,10 @@ def cube_sphere(c, i, s, j, out):  # colliders.go:369-441
         return
     cw = mul_vector(c["T"], closest)
     nrm = [cw[k] - pos[k] for k in range(3)]
-    if real_equal(magnitude(nrm), 0.0):
+    # colliders.go:417-421; with float32 values (the precision form) also when
+    # the centre needed no clamping: the reference's absolute 1e-14 is below
+    # float32's rounding of the world-space round trip
+    if real_equal(magnitude(nrm), 0.0) or (real_type(dist) is np.float32 and dist == 0.0):
         nrm = list(s["velocity"])
     vec_normalize(nrm)
     pen = r

@@ -124,16 +124,19 @@ def skew(v):  # contact.go:612-616
 
 
 # ---------------------------------------------------------------- quaternion.go
-def quat_add_scaled_vector(q, v, scale):  # quaternion.go:20-33
+def quat_scaled_increment(q, v, scale):  # quaternion.go:20-33 up to the sum
     t = [0.0, v[0] * scale, v[1] * scale, v[2] * scale]
     w = t[0] * q[0] - t[1] * q[1] - t[2] * q[2] - t[3] * q[3]
     x = t[0] * q[1] + t[1] * q[0] + t[2] * q[3] - t[3] * q[2]
     y = t[0] * q[2] + t[2] * q[0] + t[3] * q[1] - t[1] * q[3]
     z = t[0] * q[3] + t[3] * q[0] + t[1] * q[2] - t[2] * q[1]
-    q[0] += w * 0.5
-    q[1] += x * 0.5
-    q[2] += y * 0.5
-    q[3] += z * 0.5
+    return [w * 0.5, x * 0.5, y * 0.5, z * 0.5]
+
+
+def quat_add_scaled_vector(q, v, scale):  # quaternion.go:20-33
+    inc = quat_scaled_increment(q, v, scale)
+    for k in range(4):
+        q[k] += inc[k]
 
 
 def quat_normalize(q):  # quaternion.go:78-99
@@ -283,7 +286,14 @@ def _apply_position_change(c, bodies, penetration):  # contact.go:286-386
         pw, qw = b["position_w"], b["orientation_w"]
         for k in range(3):
             pw[k] += float(c.normal[k] * lin_m[i])
-        quat_add_scaled_vector(qw, [float(x) for x in ang_change[i]], 1.0)
+        if t is float:
+            quat_add_scaled_vector(qw, ang_change[i], 1.0)
+        else:
+            # the increment in float32 from the orientation rounded to float32,
+            # accumulated in float64
+            inc = quat_scaled_increment([t(x) for x in qw], ang_change[i], t(1.0))
+            for k in range(4):
+                qw[k] += float(inc[k])
         quat_normalize(qw)
         b["position"] = [t(x) for x in pw]
         b["orientation"] = [t(x) for x in qw]
@@ -314,11 +324,12 @@ def _friction_impulse(c, bodies, iits):  # contact.go:535-606
     dv[0] += inv_mass
     dv[4] += inv_mass
     dv[8] += inv_mass
-    # the inversion and the product in float64 (the precision form's island)
+    # the inversion in float64 (the precision form's island), the product in
+    # the bulk type
     t = real_type(dv[0])
-    k = m3_invert([float(x) for x in dv])
-    kill = [float(c.desired), float(-c.velocity[1]), float(-c.velocity[2])]
-    ic = [t(x) for x in m3_mul_vector(k, kill)]
+    k = [t(x) for x in m3_invert([float(x) for x in dv])]
+    kill = [c.desired, -c.velocity[1], -c.velocity[2]]
+    ic = m3_mul_vector(k, kill)
     planar = sqrt_(ic[1] * ic[1] + ic[2] * ic[2])
     if planar > ic[0] * c.friction:
         ic[1] /= planar

@@ -314,6 +314,24 @@ template <class A, class B> inline Q4<A> cq4(const Q4<B>& q) {
 }
 template <class A, class B> inline M3<A> cm3(const M3<B>& m) { M3<A> r; for (int i = 0; i < 9; ++i) r[i] = (A)m[i]; return r; }
 
+// Orientation.AddScaledVector(v, 1.0) of an orientation held in W across
+// adjustPositions (contact.go:374-375): the increment t = (0, v) * q and
+// t * 0.5 in R, from q rounded to R, added to q in W.  With R == W this is
+// AddScaledVector (quaternion.go:18-33) itself.
+template <class R, class W> inline void AddScaledVectorIsland(Q4<W>& q, const V3<R>& v) {
+  Q4<R> qr = cq4<R>(q);
+  Q4<R> t;
+  t[0] = 0.0;
+  t[1] = v[0] * (R)1.0;
+  t[2] = v[1] * (R)1.0;
+  t[3] = v[2] * (R)1.0;
+  Mul(t, qr);
+  q[0] += (W)(t[0] * (R)0.5);
+  q[1] += (W)(t[1] * (R)0.5);
+  q[2] += (W)(t[2] * (R)0.5);
+  q[3] += (W)(t[3] * (R)0.5);
+}
+
 // ---------------------------------------------------------------- rigidbody.go
 
 enum Shape : int32_t { kSphere = 0, kCube = 1 };
@@ -584,8 +602,12 @@ inline bool CubeSphere(const Body<R, W>& cube, int ci, const Body<R, W>& sphere,
   c.point = closestWorld;
   c.normal = closestWorld;
   Sub(c.normal, position);
-  if (RealEqual<R>(Magnitude(c.normal), (R)0.0)) {
-    c.normal = sphere.velocity;  // colliders.go:417-421
+  // colliders.go:417-421.  The reference tests the world-space round trip
+  // against RealEqual's absolute 1e-14, which float32 rounding exceeds, so
+  // the precision form (R = float) also takes the fallback when the centre
+  // needed no clamping (it lies in the box: the box-space distance is zero).
+  if (RealEqual<R>(Magnitude(c.normal), (R)0.0) || (sizeof(R) < sizeof(double) && dist == (R)0)) {
+    c.normal = sphere.velocity;
   }
   Normalize(c.normal);
   c.penetration = sphere.radius;
@@ -939,8 +961,9 @@ template <class R, class W> struct Resolver {
       pw[1] += (W)(c.normal[1] * linearMove[i]);
       pw[2] += (W)(c.normal[2] * linearMove[i]);
       // Orientation.AddScaledVector(angularChange, 1.0); Orientation.Normalize()
+      // the increment in R from the orientation rounded to R, accumulated in W
       Q4<W>& qw = oriW[c.body[i]];
-      AddScaledVector(qw, cv3<W>(angularChange[i]), (W)1.0);
+      AddScaledVectorIsland<R, W>(qw, angularChange[i]);
       Normalize(qw);
       body.position = cv3<R>(pw);
       body.orientation = cq4<R>(qw);
@@ -1012,9 +1035,10 @@ template <class R, class W> struct Resolver {
     dv[0] += inverseMass;
     dv[4] += inverseMass;
     dv[8] += inverseMass;
-    M3<W> impulseMatrix = Invert(cm3<W>(dv));
-    V3<W> velKill = mk3<W>((W)c.desiredDeltaVelocity, (W)-c.contactVelocity[1], (W)-c.contactVelocity[2]);
-    V3<R> ic = cv3<R>(MulVector3(impulseMatrix, velKill));
+    // the inversion in W; the solve in R
+    M3<R> impulseMatrix = cm3<R>(Invert(cm3<W>(dv)));
+    V3<R> velKill = mk3<R>(c.desiredDeltaVelocity, -c.contactVelocity[1], -c.contactVelocity[2]);
+    V3<R> ic = MulVector3(impulseMatrix, velKill);
     R planar = Sqrt<R>(ic[1] * ic[1] + ic[2] * ic[2]);
     if (planar > ic[0] * c.friction) {
       ic[1] /= planar;

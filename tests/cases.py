@@ -59,6 +59,16 @@ def sphere_inside_cube():
                   dict(shape="sphere", pos=(0.2, 5.0, 0.0), r=0.5, vel=(0.0, -2.0, 0.0))], FAR_PLANE)
 
 
+def sphere_inside_turned_cube_far():
+    """A sphere centre inside a turned box 20 m from the origin: the world-space
+    round trip of the centre is off by float32 rounding (about 1e-6), far above
+    RealEqual's absolute 1e-14, so the precision form decides the fallback by
+    the clamp (colliders.go:414-421)."""
+    q = quat_axis(0.7, (0.3, 1.0, -0.4))
+    return world([dict(shape="cube", pos=(4.98, 19.37, -1.04), half=(0.93, 0.52, 0.89), quat=q),
+                  dict(shape="sphere", pos=(5.3, 19.45, -0.72), r=0.48, vel=(-1.7, -2.13, 0.81))], FAR_PLANE)
+
+
 def cube_on_cube():
     # B (h=0.5) rotated 45 deg about z, resting a vertex... an edge into A's top face
     return world([dict(shape="cube", pos=(0.0, 5.0, 0.0), half=(1.0, 1.0, 1.0)),
@@ -140,7 +150,8 @@ def static_cube_singular_friction():
 
 
 ALL = {"cube_resting": cube_resting, "sphere_resting": sphere_resting, "sphere_pair": sphere_pair,
-       "cube_sphere": cube_sphere, "sphere_inside_cube": sphere_inside_cube, "cube_on_cube": cube_on_cube,
+       "cube_sphere": cube_sphere, "sphere_inside_cube": sphere_inside_cube,
+       "sphere_inside_turned_cube_far": sphere_inside_turned_cube_far, "cube_on_cube": cube_on_cube,
        "cube_edge_edge": cube_edge_edge, "tilted_cube_on_plane": tilted_cube_on_plane,
        "cube_edge_down": cube_edge_down, "cube_below_plane": cube_below_plane,
        "static_cube_singular_friction": static_cube_singular_friction,

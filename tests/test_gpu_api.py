@@ -255,3 +255,31 @@ def test_kernel_launch_accounting(cuda_lib):
     before = _lib.kernel_launches()
     b.step(10, DT)
     assert _lib.kernel_launches() - before == 10 * 4  # integrate, narrowphase, resolve, queue reorder
+
+
+@pytest.mark.parametrize("form", [0, 1])
+def test_bounded_wait_gives_up_and_the_batch_steps_on(form, cuda_lib):
+    """The narrowphase's one device wait (bulk copies of each world's bodies
+    completing on an mbarrier) runs out: the test hook makes it expect 16
+    bytes more than it copies, so every real copy lands and nothing is in
+    flight when it gives up after 64 polls.  The call reports CZ_ERR_TIMEOUT;
+    with the hook off the batch steps on, bit for bit with the oracle."""
+    from cubez_gb300 import CubezError
+    from cubez_gb300.batch import WorldBatch
+    sc = scenes.mixed(num_worlds=8, seed=35)
+    b = WorldBatch.from_scene(sc, form=form)
+    ref = OracleBatch(sc, form=form)
+    b.step(3, DT)
+    ref.step(3, DT)
+    assert b.L.cz_set_wait_test(b.h, 16, 64) == 0
+    with pytest.raises(CubezError) as e:
+        b.narrowphase()
+    assert e.value.status == 6  # CZ_ERR_TIMEOUT
+    assert np.any(b.stats()["status"] & 8)  # the worlds whose wait gave up are flagged
+    assert b.L.cz_set_wait_test(b.h, 0, 0) == 0
+    assert b.L.cz_set_wait_test(b.h, -1, 0) == 1
+    b.step(3, DT)
+    ref.step(3, DT)
+    g, r = b.download(), ref.bodies()
+    for k in ("position", "orientation", "velocity", "rotation"):
+        np.testing.assert_array_equal(g[k], r[k], err_msg=k)

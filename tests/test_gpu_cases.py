@@ -26,6 +26,7 @@ DT = 1.0 / 60.0
 # branch each scene must take, per form (None: the same in both)
 EXPECTED = {
     "sphere_inside_cube": {"sphere_centre_in_box"},
+    "sphere_inside_turned_cube_far": {"sphere_centre_in_box"},
     "cube_edge_edge": {"edge_cross"},
     "cube_on_cube": {"vertex_face", "vertex_face_swapped"},
     "edge_parallel_fallback": ({"edge_cross"}, {"edge_parallel"}),

@@ -60,3 +60,21 @@ def test_piles_full_size_one_frame(cuda_lib):
     gs, rs = gpu.stats(), ref.stats()
     assert rs["contacts"].min() > 1000
     np.testing.assert_array_equal(gs["vel_iterations"], rs["vel_iterations"])
+
+
+def test_batched_workload_full_size(cuda_lib):
+    """The batched configuration: 4096 worlds of U{8..64} spheres and cubes in
+    the plain float64 form, three frames from a settled state, bit for bit
+    (the step order of examples/cubedrop.go:29-75 in every world)."""
+    scene = scenes.mixed(num_worlds=4096, seed=2)
+    gpu, ref, _ = _settled_pair(scene, 0, settle=150)
+    threads = hardware_threads()
+    for _ in range(3):
+        gpu.step(1, DT)
+        ref.step(1, DT, 4, threads)
+    assert_bodies_equal(gpu.download(), ref.bodies())
+    gs, rs = gpu.stats(), ref.stats()
+    assert rs["contacts"].sum() > 100_000
+    np.testing.assert_array_equal(gpu.contact_counts(), rs["contacts"])
+    np.testing.assert_array_equal(gs["pos_iterations"], rs["pos_iterations"])
+    np.testing.assert_array_equal(gs["vel_iterations"], rs["vel_iterations"])

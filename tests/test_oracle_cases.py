@@ -159,7 +159,8 @@ def test_cases_match_second_restatement(name, form):
         assert [float(x) for x in p] == want["point"][k].tolist()
         assert [float(x) for x in n] == want["normal"][k].tolist()
         assert float(pen) == want["penetration"][k]
-    expect = {"sphere_inside_cube": {"sphere_centre_in_box"}, "cube_edge_edge": {"edge_cross"},
+    expect = {"sphere_inside_cube": {"sphere_centre_in_box"}, "sphere_inside_turned_cube_far": {"sphere_centre_in_box"},
+              "cube_edge_edge": {"edge_cross"},
               "cube_on_cube": {"vertex_face", "vertex_face_swapped"},
               "edge_parallel_fallback": [{"edge_cross"}, {"edge_parallel"}][form],
               "edge_range_fallback": [{"edge_cross"}, {"edge_out_of_range"}][form]}.get(name, set())
