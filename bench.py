@@ -190,8 +190,8 @@ def _alg_bytes(phase, real, nbodies, counters, frames, rollouts):
     launches = frames * rollouts
     contacts = counters["contacts"] / launches
     resolved = counters["contacts_resolved"] / launches
-    if phase == 0:  # integrate: read 13 state + 3 acc + 9+9 inertia + 3 scalars, write 13 + 3 + 9; 2 flag bytes
-        return nbodies * (62 * real + 2)
+    if phase == 0:  # integrate: 13 state reals read and written, a symmetric inverse inertia (6) read and one written
+        return nbodies * 38 * real
     if phase == 1:  # narrowphase: stage 11 rows + shape, write contacts (9 reals + packed bodies)
         return nbodies * (11 * real + 4) + contacts * (9 * real + 4)
     # resolver: bodies in (27 reals + flag) and out (23 reals + flag), contacts in
@@ -333,6 +333,9 @@ def run_ours(args):
         pl = ph[i] / frames
         kernels[n] = {"ms_per_launch": pl, "share": ph[i] / sum(ph), "alg_bytes_per_launch": bl,
                       "gbs": bl / (pl / 1e3) / 1e9}
+        if i == 0:  # what the kernel moves: 37 reals + 2 flag bytes read, 25 reals written
+            kernels[n]["moved_bytes_per_launch"] = nb * (62 * real + 2)
+            kernels[n]["moved_gbs"] = nb * (62 * real + 2) / (pl / 1e3) / 1e9
     info = batches[head].info()
     for b in batches.values():
         b.close()
@@ -510,8 +513,11 @@ def run_piles(args):
     units = nw * (n * (n - 1) + n)  # ordered pair tests + half-space tests per frame
     out = {}
     settled = None
+    fixed = json.loads(args.tuning) if args.tuning else None
     for name, form in (("fp32", FORM_FP32), ("fp64", FORM_FP64)):
         b = WorldBatch.from_scene(scene, form=form, device=local)
+        if fixed:
+            b.set_tuning(**fixed)
         b.prepare_rollout(frames, DT)
         b.snapshot()
         for _ in range(args.warmup if args.warmup_given else 0):
@@ -583,6 +589,14 @@ def run_batched(args):
     fixed = json.loads(args.tuning) if args.tuning else None
     if fixed:
         b.set_tuning(**fixed)
+    elif args.autotune:
+        from cubez_gb300 import autotune
+        # tune on a settled state (half-way through the rollout), untimed
+        b.step(frames // 2, DT)
+        b.snapshot()
+        autotune.tune(b, frames=args.tune_frames, dt=DT)
+        b.upload(scene)
+    tuning = b.get_tuning()
     b.prepare_rollout(frames, DT)
     b.snapshot()
 
@@ -667,7 +681,7 @@ def run_batched(args):
                        "l2": "explicit 252 MB flush before every timed rollout"},
             "world_steps_per_s": nw * frames * ws / (ms / 1e3), "phase_ms": (ph / args.steps).tolist(),
             "counters_per_frame": per, "gpu_launches": launches, "clocks": clocks.summary(), "e2e": e2e,
-            "batch": info, "cpu_baseline": cpu}
+            "batch": info, "tuning": tuning, "cpu_baseline": cpu}
     print(json.dumps(line))
 
 

@@ -406,7 +406,8 @@ int configure(cz_batch* b) {
     return fail(CZ_ERR_BODY_LIMIT, "world too large for the shared-memory tiles");
   CZ_CUDA(b->ops->prepare(b->np_smem, b->rs_smem, b->rs_lanes));
   int npb = 0, rsb = 0;
-  CZ_CUDA(b->ops->occupancy(&npb, b->np_threads, b->np_smem, &rsb, b->rs_smem, b->rs_lanes, b->mode));
+  CZ_CUDA(b->ops->occupancy(&npb, b->np_threads, b->np_smem, &rsb, b->rs_smem, b->rs_lanes, b->mode,
+                            b->grid_min_bodies > 0 && b->max_n >= b->grid_min_bodies));
   npb = std::max(npb, 1);
   rsb = std::max(rsb, 1);
   if (b->rs_ctas_per_sm > 0) rsb = std::min(rsb, b->rs_ctas_per_sm);
@@ -509,8 +510,11 @@ int cz_batch_create(const cz_batch_desc* d, cz_batch** out) {
   b->nsmall = b->num_worlds - (int)b->big_ids.size();
   b->rs_nbs = (int)std::max<long long>(round_up(max_small, 4), 4);
   b->np_threads = b->max_n >= 256 ? 256 : 128;
-  b->rs_cs = d->form == CZ_FORM_FP64 ? 96 : 128;
-  b->rs_lanes = d->form == CZ_FORM_FP64 ? 4 : 8;
+  // defaults from the tuned precision workload: a world per warp in float32;
+  // two per warp in float64, which shares their float64 chains (the tuner
+  // may change both)
+  b->rs_cs = 96;
+  b->rs_lanes = d->form == CZ_FORM_FP64 ? 16 : 32;
   // world queue: decreasing body count (pair work grows as n^2)
   std::vector<int> order(b->num_worlds);
   std::iota(order.begin(), order.end(), 0);

@@ -218,9 +218,17 @@ static cudaError_t raise_smem_limit(const void* f, size_t bytes) {
   return cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
 }
 
+// The narrowphase instantiation a batch runs: with the grid only when one of
+// its worlds is large enough for it.
+static bool uses_grid(const HostView& h) { return h.grid_min_bodies > 0 && h.max_bodies >= h.grid_min_bodies; }
+static const void* narrowphase_fn(bool grid) {
+  return grid ? (const void*)k_narrowphase<R, true> : (const void*)k_narrowphase<R, false>;
+}
+
 static cudaError_t prepare(size_t np, size_t rs, int lanes) {
-  cudaError_t e = raise_smem_limit((const void*)k_narrowphase<R>, np);
+  cudaError_t e = raise_smem_limit(narrowphase_fn(false), np);
   if (e != cudaSuccess) return e;
+  if ((e = raise_smem_limit(narrowphase_fn(true), np)) != cudaSuccess) return e;
   for (int mode = 0; mode <= 1; ++mode) {
     const void* f = resolve_fn_mode(lanes, mode);
     if (!f) return cudaErrorInvalidValue;
@@ -237,7 +245,10 @@ static cudaError_t integrate(const HostView& h, double dt, double bias, int thre
 }
 
 static cudaError_t narrowphase(const HostView& h, int nbs, int threads, int grid, size_t smem, cudaStream_t s) {
-  k_narrowphase<R><<<grid, threads, smem, s>>>(view_of(h), nbs);
+  if (uses_grid(h))
+    k_narrowphase<R, true><<<grid, threads, smem, s>>>(view_of(h), nbs);
+  else
+    k_narrowphase<R, false><<<grid, threads, smem, s>>>(view_of(h), nbs);
   return cudaGetLastError();
 }
 
@@ -327,8 +338,9 @@ static cudaError_t download(const HostView& h, double* sg, uint8_t* u8, int* i32
   return cudaGetLastError();
 }
 
-static cudaError_t occupancy(int* npb, int np_threads, size_t nps, int* rsb, size_t rss, int lanes, int mode) {
-  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(npb, k_narrowphase<R>, np_threads, nps);
+static cudaError_t occupancy(int* npb, int np_threads, size_t nps, int* rsb, size_t rss, int lanes, int mode,
+                             int grid) {
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(npb, narrowphase_fn(grid != 0), np_threads, nps);
   if (e != cudaSuccess) return e;
   const void* f = resolve_fn_mode(lanes, mode);  // the instantiation that runs (registers differ)
   if (!f) return cudaErrorInvalidValue;

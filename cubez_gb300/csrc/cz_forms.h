@@ -102,7 +102,7 @@ struct FormOps {
   cudaError_t (*download)(const HostView& v, double* stage, uint8_t* u8, int* i32, const int* h2p, int nb,
                           double* off, cudaStream_t s);
   cudaError_t (*occupancy)(int* np_blocks, int np_threads, size_t np_smem, int* rs_blocks, size_t rs_smem,
-                           int lanes, int mode);
+                           int lanes, int mode, int grid);
   // contacts: device rows <-> AoS doubles staging (10 doubles + 2 ints per contact)
   cudaError_t (*contacts_out)(const HostView& v, long long start, int count, double* stage, int* bodies,
                               cudaStream_t s);

@@ -830,7 +830,9 @@ __device__ int np_grid_units(const NPTile<R>& tl, const BatchView<R>& v, const N
   return cnt;
 }
 
-template <class R>
+// GRID = false compiles the all-pairs path alone (worlds too small for the
+// grid), so its registers and occupancy stay those of that path.
+template <class R, bool GRID>
 __global__ void __launch_bounds__(256) k_narrowphase(BatchView<R> v, int nbs) {
   extern __shared__ __align__(128) unsigned char smem[];
   unsigned long long* bar = reinterpret_cast<unsigned long long*>(smem);
@@ -907,7 +909,7 @@ __global__ void __launch_bounds__(256) k_narrowphase(BatchView<R> v, int nbs) {
     int out = 0, nsurv = 0;
     uint32_t err = 0;
     const NPGrid g = np_grid_scratch(tl);
-    if (v.grid_min_bodies > 0 && n >= v.grid_min_bodies && np_grid_build(tl, n, g, scan, chunk_parity)) {
+    if (GRID && v.grid_min_bodies > 0 && n >= v.grid_min_bodies && np_grid_build(tl, n, g, scan, chunk_parity)) {
       // Grid: each body's kept units (counted, then listed and sorted), as
       // many bodies at a time as the list holds, then their full tests.
       for (int ib = 0; ib < n;) {

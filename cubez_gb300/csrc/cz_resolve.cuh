@@ -119,9 +119,29 @@ __device__ __forceinline__ unsigned key_of(float v, float eps) {
   return (b > e && b <= 0x7F800000) ? (unsigned)b : 0u;
 }
 
+// The first maximum over a whole warp by warp reductions (redux.sync): the
+// largest key, then the smallest index among the lanes holding it; a 64-bit
+// key is reduced by its high half, then its low half.
+__device__ __forceinline__ void warp_first_max(unsigned& key, int& idx) {
+  const unsigned m = __reduce_max_sync(0xffffffffu, key);
+  idx = (int)__reduce_min_sync(0xffffffffu, key == m ? (unsigned)idx : 0xffffffffu);
+  key = m;
+}
+__device__ __forceinline__ void warp_first_max(unsigned long long& key, int& idx) {
+  const unsigned hi = (unsigned)(key >> 32), lo = (unsigned)key;
+  const unsigned mh = __reduce_max_sync(0xffffffffu, hi);
+  const unsigned ml = __reduce_max_sync(0xffffffffu, hi == mh ? lo : 0u);
+  idx = (int)__reduce_min_sync(0xffffffffu, (hi == mh && lo == ml) ? (unsigned)idx : 0xffffffffu);
+  key = ((unsigned long long)mh << 32) | ml;
+}
+
 // Largest key over the G lanes of a group, smallest index among equal keys
 // (the first maximum of the reference's scan, contact.go:238-245, 394-402).
-template <int G, class K> __device__ __forceinline__ void group_first_max(K& key, int& idx) {
+template <int G, bool REDUX = true, class K> __device__ __forceinline__ void group_first_max(K& key, int& idx) {
+  if constexpr (G == 32 && REDUX) {
+    warp_first_max(key, idx);
+    return;
+  }
 #pragma unroll
   for (int off = G / 2; off > 0; off >>= 1) {
     const K ok = __shfl_xor_sync(0xffffffffu, key, off);
@@ -824,7 +844,7 @@ __device__ int velocity_loop(const RCtx<R, W>& x, const BatchView<R>& v, int w, 
       }
     }
   while (__any_sync(FULL, run)) {
-    group_first_max<G>(best, bidx);
+    group_first_max<G, !LEARN>(best, bidx);
     if (best == 0) run = false;
     if (run && gl == 0) {
       match_awake(x, x.cb[bidx]);
@@ -859,7 +879,7 @@ __device__ int velocity_loop(const RCtx<R, W>& x, const BatchView<R>& v, int w, 
 // compiles the plain resolver alone (v.mode is ignored), so the learned paths
 // cost the plain kernel no registers.
 template <class R, class W, int G, bool LEARN>
-__global__ void __launch_bounds__(32, LEARN ? 9 : 0) k_resolve(BatchView<R> v, int nbs, int cs, R dt) {
+__global__ void __launch_bounds__(32, LEARN ? (G == 32 ? 18 : 16) : 0) k_resolve(BatchView<R> v, int nbs, int cs, R dt) {
   constexpr int NG = 32 / G;
   extern __shared__ __align__(128) unsigned char smem[];
   const int lane = threadIdx.x;
@@ -925,7 +945,7 @@ __global__ void __launch_bounds__(32, LEARN ? 9 : 0) k_resolve(BatchView<R> v, i
         }
       }
     while (__any_sync(FULL, run)) {
-      group_first_max<G>(best, bidx);
+      group_first_max<G, !LEARN>(best, bidx);
       if (best == 0) run = false;
       if (run && gl == 0) match_awake(x, x.cb[bidx]);
       __syncwarp();

@@ -95,3 +95,49 @@ def test_culled_pairs_have_no_contact(kinds):
         cr.check_for_collisions(b, 1, a, 0, out)
         assert not out, "trial %d: a culled pair has %d contacts" % (trial, len(out))
     assert culled > 1000
+
+
+def _plane_rejects(b, plane):
+    """The half-space cull of k_narrowphase (plane_culled) for body b."""
+    n = [F(x) for x in plane[:3]]
+    off = F(plane[3])
+    c = [F(x) for x in cr.get_axis(b["T"], 3)]
+    d = n[0] * c[0] + n[1] * c[1] + n[2] * c[2]
+    nlen = np.sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]) * F(1.0001)
+    rb, _ = _cull_radii(b)
+    r = rb if b["shape"] == cr.SPHERE else rb * nlen
+    scale = F(1) + (abs(c[0]) + abs(c[1]) + abs(c[2])) * nlen + abs(off)
+    return bool(d - r > off + F(1e-3) + F(1e-5) * scale), float(r)
+
+
+@pytest.mark.parametrize("shape", [cr.CUBE, cr.SPHERE])
+def test_culled_plane_units_have_no_contact(shape):
+    """Bodies just above the half-space cull's threshold, for tilted planes
+    with non-unit normals and offsets too: the reference's
+    CheckAgainstHalfSpace (colliders.go:180-207, 308-366) finds no contact."""
+    rng = np.random.default_rng(23 + shape)
+    culled = 0
+    for trial in range(2000):
+        nrm = rng.normal(0, 1, 3)
+        nrm *= rng.uniform(0.5, 2.0) / np.linalg.norm(nrm)
+        plane = [float(nrm[0]), float(nrm[1]), float(nrm[2]), float(rng.uniform(-30, 30))]
+        b = _body(rng, shape, [0.0, 0.0, 0.0], _quat(rng))
+        _, r = _plane_rejects(b, plane)
+        # centre at a height just past the threshold along the normal, far off the origin sideways
+        side = rng.normal(0, 1, 3) * rng.uniform(0, 40)
+        side -= nrm * (side @ nrm) / (nrm @ nrm)
+        height = (plane[3] + r + 1e-3) * (1.0 + rng.uniform(1e-6, 3e-3)) + rng.uniform(0, 2e-3)
+        centre = nrm / (nrm @ nrm) * height + side
+        b["position"] = centre.tolist()
+        b["T"] = cr.collider_transform(b)
+        rej, _ = _plane_rejects(b, plane)
+        if not rej:
+            continue
+        culled += 1
+        out = []
+        if shape == cr.SPHERE:
+            cr.sphere_half_space(b, 0, plane, out)
+        else:
+            cr.cube_half_space(b, 0, plane, out)
+        assert not out, "trial %d: a culled half-space test has %d contacts" % (trial, len(out))
+    assert culled > 1000
