@@ -497,6 +497,12 @@ __device__ __forceinline__ void load_bodies(const RCtx<R, W>& x, const BatchView
 // broadcast scratch, packed bodies, awake flags.  The learned paths keep
 // their per-body scratch and the impulse rows in global memory, so they use
 // the same slot (and reach the same occupancy) as the plain resolver.
+// The float64 form with one world per warp gathers the contacts touching the
+// two resolved bodies before updating them (see position_loop_w); room for
+// one gather.
+constexpr int kTouchList = 64;
+template <class R> __host__ __device__ constexpr bool gathers_updates() { return sizeof(R) == 8; }
+
 template <class R, class W> __host__ __device__ inline size_t rs_slot_bytes(int nbs, int cs) {
   const size_t nb16 = (size_t)((nbs + 15) & ~15);
   size_t b = (size_t)7 * nbs * sizeof(W);
@@ -505,11 +511,13 @@ template <class R, class W> __host__ __device__ inline size_t rs_slot_bytes(int 
   b += 16 * sizeof(R);
   b += (size_t)cs * sizeof(int);
   b += nb16;
+  if (gathers_updates<R>()) b += (size_t)kTouchList * sizeof(int);
   return (b + 15) & ~(size_t)15;
 }
 
 template <class R, class W> struct Slot {
   RCtx<R, W> x;
+  int* ml;          // [kTouchList] contacts touching the two bodies just resolved (float64 form)
   R* cw_s;
   int* cb_s;
   uint8_t* aw_pos;  // awake flags at the start of adjustVelocities (global)
@@ -528,6 +536,7 @@ __device__ __forceinline__ Slot<R, W> make_slot(unsigned char* base, int nbs, in
   x.bc = s.cw_s + (size_t)w_rows_kept<R>() * cs;
   s.cb_s = reinterpret_cast<int*>(x.bc + 16);
   x.aw = reinterpret_cast<uint8_t*>(s.cb_s + cs);
+  s.ml = reinterpret_cast<int*>(x.aw + ((nbs + 15) & ~15));
   x.save = x.delta = x.jw = nullptr;
   x.wi = nullptr;
   x.wst = x.jst = 0;
@@ -873,13 +882,112 @@ __device__ int velocity_loop(const RCtx<R, W>& x, const BatchView<R>& v, int w, 
   return used;
 }
 
+// ---------------------------------------------------------------- gathered updates
+// The float64 form with one world per warp updates, after a resolved
+// contact, only the contacts touching its two bodies: gathered in contact
+// order (a ballot per 32 contacts) and updated one per lane, instead of every
+// lane walking all its contacts, where a matching contact's float64 update
+// ran once per loop position with a match anywhere in the warp, at the cost
+// of a whole warp instruction on the float64 pipe for each.  The reference's
+// loop visits every contact but changes only these, and each update touches
+// only its own contact (contact.go:254-280, 412-440), so the result is the
+// same bit for bit.  (In float32 the gather did not pay: the same number of
+// instructions, and more registers.)
+
+// Applies upd(k) to every contact k touching body d0 or d1.
+template <class R, class W, class F>
+__device__ __forceinline__ void update_touching(const RCtx<R, W>& x, int C, int lane, int d0, int d1, int* ml,
+                                                F&& upd) {
+  int m = 0;
+  for (int base = 0; base < C; base += 32) {
+    const int k = base + lane;
+    bool hit = false;
+    if (k < C) {
+      const int bb = x.cb[k];
+      const int kb0 = body0_of(bb), kb1 = body1_of(bb);
+      hit = kb0 == d0 || (d1 >= 0 && kb0 == d1) || (kb1 >= 0 && (kb1 == d0 || kb1 == d1));
+    }
+    const unsigned bal = __ballot_sync(FULL, hit);
+    if (hit) ml[m + __popc(bal & ((1u << lane) - 1u))] = k;
+    m += __popc(bal);
+    if (m > kTouchList - 32 || base + 32 >= C) {
+      __syncwarp();
+      for (int j = lane; j < m; j += 32) upd(ml[j]);
+      __syncwarp();
+      m = 0;
+    }
+  }
+}
+
+// The warp's first maximum of a row's keys (W_PEN or W_DDV) over the world's
+// contacts.
+template <class R, class W>
+__device__ __forceinline__ void warp_row_first_max(const RCtx<R, W>& x, int row, int C, int lane,
+                                                   decltype(key_of((R)0, (R)0))& best, int& bidx) {
+  best = key_of((R)0, (R)0);
+  bidx = 0x7fffffff;
+  for (int k = lane; k < C; k += 32) {
+    const auto key = key_of(x.Cf(row, k), (R)0.01);
+    if (key > best) {
+      best = key;
+      bidx = k;
+    }
+  }
+  warp_first_max(best, bidx);
+}
+
+// adjustPositions (contact.go:231-283), one world per warp, gathered updates.
+template <class R, class W>
+__device__ int position_loop_w(const RCtx<R, W>& x, const BatchView<R>& v, int bstart, int C, int lane, int max_it,
+                               bool run, int* ml) {
+  int used = 0;
+  while (run) {
+    decltype(key_of((R)0, (R)0)) best;
+    int bidx;
+    warp_row_first_max(x, W_PEN, C, lane, best, bidx);
+    if (best == 0) break;
+    if (lane == 0) match_awake(x, x.cb[bidx]);
+    __syncwarp();
+    apply_position_change<R, W, 32>(x, v, bstart, bidx, true, lane);
+    __syncwarp();
+    const int rb = x.cb[bidx];
+    const int d0 = body0_of(rb), d1 = body1_of(rb);
+    update_touching(x, C, lane, d0, d1, ml, [&](int k) { penetration_update(x, k, d0, d1); });
+    if (++used >= max_it) break;
+  }
+  return used;
+}
+
+// adjustVelocities (contact.go:388-445), one world per warp, gathered updates.
+template <class R, class W, bool LEARN>
+__device__ int velocity_loop_w(const RCtx<R, W>& x, const BatchView<R>& v, int w, int C, int lane, int max_it,
+                               bool run, int* ml) {
+  int used = 0;
+  while (run) {
+    decltype(key_of((R)0, (R)0)) best;
+    int bidx;
+    warp_row_first_max(x, W_DDV, C, lane, best, bidx);
+    if (best == 0) break;
+    if (lane == 0) {
+      match_awake(x, x.cb[bidx]);
+      apply_velocity_change<R, W, LEARN>(x, v, w, bidx);
+    }
+    __syncwarp();
+    const int rb = x.cb[bidx];
+    const int d0 = body0_of(rb), d1 = body1_of(rb);
+    update_touching(x, C, lane, d0, d1, ml, [&](int k) { velocity_update(x, k, d0, d1); });
+    if (++used >= max_it) break;
+  }
+  return used;
+}
+
 // v.mode: 0 plain, 1 harvest (plain, copying k_warm_features' features and
 // writing the applied impulses), 2 learned warm start (applying
 // k_warm_features' plan) with fallback to the plain solve.  LEARN = false
 // compiles the plain resolver alone (v.mode is ignored), so the learned paths
 // cost the plain kernel no registers.
 template <class R, class W, int G, bool LEARN>
-__global__ void __launch_bounds__(32, LEARN ? (G == 32 ? 18 : 16) : 0) k_resolve(BatchView<R> v, int nbs, int cs, R dt) {
+__global__ void __launch_bounds__(32, LEARN ? (G == 32 && sizeof(R) == 4 ? 18 : 16) : 0) k_resolve(BatchView<R> v, int nbs, int cs, R dt) {
   constexpr int NG = 32 / G;
   extern __shared__ __align__(128) unsigned char smem[];
   const int lane = threadIdx.x;
@@ -930,8 +1038,12 @@ __global__ void __launch_bounds__(32, LEARN ? (G == 32 ? 18 : 16) : 0) k_resolve
       for (int k = gl; k < C; k += G) prepare_contact(x, v, cst + k, k);
     __syncwarp();
     const int max_it = v.max_iterations >= 0 ? v.max_iterations : C * v.iter_mult;
+    constexpr bool kGather = G == 32 && gathers_updates<R>();
     // ---------------- adjustPositions, contact.go:231-283
     int used = 0;
+    if constexpr (kGather) {
+      used = position_loop_w(x, v, bstart, C, lane, max_it, active && max_it > 0, sl.ml);
+    } else {
     bool run = active && max_it > 0;
     // as in velocity_loop: the update pass also finds the next argmax
     auto best = key_of((R)0, (R)0);
@@ -969,6 +1081,7 @@ __global__ void __launch_bounds__(32, LEARN ? (G == 32 ? 18 : 16) : 0) k_resolve
       if (run && ++used >= max_it) run = false;
       best = nbest;
       bidx = nidx;
+    }
     }
     const int pos_used = used;
     const bool solve = active && max_it > 0;
@@ -1021,7 +1134,10 @@ __global__ void __launch_bounds__(32, LEARN ? (G == 32 ? 18 : 16) : 0) k_resolve
       warmed = group_sum<G>(nw) > 0;
     }
     // ---------------- adjustVelocities, contact.go:388-445
-    used = velocity_loop<R, W, G, LEARN>(x, v, w, C, gl, max_it, solve);
+    if constexpr (kGather)
+      used = velocity_loop_w<R, W, LEARN>(x, v, w, C, lane, max_it, solve, sl.ml);
+    else
+      used = velocity_loop<R, W, G, LEARN>(x, v, w, C, gl, max_it, solve);
     int vel_used = used;
     if (LEARN && mode == 2) {
       // the plain resolver has the last word: a warm-started world that used
@@ -1057,7 +1173,11 @@ __global__ void __launch_bounds__(32, LEARN ? (G == 32 ? 18 : 16) : 0) k_resolve
           x.aw = aw_now;
         }
         __syncwarp();
-        const int used2 = velocity_loop<R, W, G, LEARN>(x, v, w, C, gl, max_it, fb);
+        int used2;
+        if constexpr (kGather)
+          used2 = velocity_loop_w<R, W, LEARN>(x, v, w, C, lane, max_it, fb, sl.ml);
+        else
+          used2 = velocity_loop<R, W, G, LEARN>(x, v, w, C, gl, max_it, fb);
         if (fb) vel_used += used2;
         if (fb && gl == 0) atomicAdd(&v.counters[4], 1ull);
       }
