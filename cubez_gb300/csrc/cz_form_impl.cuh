@@ -103,7 +103,7 @@ __global__ void k_upload(BatchView<R> v, const double* __restrict__ sg, const ui
   } else {
     // RigidBody.CalculateDerivedData, rigidbody.go:268-272
     q4<W> qw = cvtq<W>(q);
-    qnormalize(qw);
+    qnormalize_island<R, W>(qw);
     q = cvtq<R>(qw);
     R rm[9];
     rotation_of(q, rm);

@@ -53,7 +53,7 @@ __global__ void __launch_bounds__(256) k_integrate(BatchView<R> v, R dt, R sleep
   add_scaled_vector(q, rot, dt);
   // CalculateDerivedData: renormalise (island type), transform, world inertia
   q4<W> qw = cvtq<W>(q);
-  qnormalize(qw);
+  qnormalize_island<R, W>(qw);
   q = cvtq<R>(qw);
   R rm[9];
   rotation_of(q, rm);

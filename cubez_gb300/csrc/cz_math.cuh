@@ -55,12 +55,48 @@ template <class R> struct m3 {
   R m[9];
 };
 
+// float <-> double conversions by integer operations for the common cases
+// (normal values and zeros; exact widening, round-to-nearest-even
+// narrowing, as the conversion instructions), the conversion instruction
+// for the rest.  On GB300 a conversion instruction has the latency of a
+// float64 operation (about 80 cycles) and shares its slow pipe; these run on
+// the integer pipe.  Same bits either way.
+__device__ __forceinline__ double widen(float f) {
+  const unsigned b = __float_as_uint(f);
+  const unsigned e = (b >> 23) & 0xffu, m = b & 0x7fffffu, sign = b & 0x80000000u;
+  if (e - 1u < 254u) return __hiloint2double((int)(sign | ((e + 896u) << 20) | (m >> 3)), (int)(m << 29));
+  if ((b << 1) == 0u) return __hiloint2double((int)sign, 0);
+  return (double)f;  // subnormal, infinite or NaN
+}
+__device__ __forceinline__ float narrow(double d) {
+  const unsigned hi = (unsigned)__double2hiint(d), lo = (unsigned)__double2loint(d);
+  const unsigned e = (hi >> 20) & 0x7ffu, sign = hi & 0x80000000u;
+  if (e - 897u < 254u) {  // a normal float (or, rounding up from the top binade, infinity)
+    unsigned r = ((e - 896u) << 23) | ((hi & 0xfffffu) << 3) | (lo >> 29);
+    const unsigned rest = lo & 0x1fffffffu;
+    r += (rest > 0x10000000u || (rest == 0x10000000u && (r & 1u))) ? 1u : 0u;
+    return __uint_as_float(sign | r);
+  }
+  if (((hi << 1) | lo) == 0u) return __uint_as_float(sign);
+  return __double2float_rn(d);  // subnormal or out of range, infinite or NaN
+}
+// The integer-pipe conversion, for the sequential chain of adjustPositions
+// (elsewhere the instruction: inlined everywhere, these cost registers).
+template <class A, class B> __device__ __forceinline__ A cvt_fast(B x) {
+  if constexpr (sizeof(A) == 8 && sizeof(B) == 4)
+    return widen(x);
+  else if constexpr (sizeof(A) == 4 && sizeof(B) == 8)
+    return narrow(x);
+  else
+    return (A)x;
+}
+
 template <class R> __device__ __forceinline__ v3<R> V(R x, R y, R z) { return v3<R>{x, y, z}; }
 template <class A, class B> __device__ __forceinline__ v3<A> cvt(const v3<B>& v) {
-  return v3<A>{(A)v.x, (A)v.y, (A)v.z};
+  return v3<A>{(A)(v.x), (A)(v.y), (A)(v.z)};
 }
 template <class A, class B> __device__ __forceinline__ q4<A> cvtq(const q4<B>& q) {
-  return q4<A>{(A)q.w, (A)q.x, (A)q.y, (A)q.z};
+  return q4<A>{(A)(q.w), (A)(q.x), (A)(q.y), (A)(q.z)};
 }
 
 // vector.go:40-47
@@ -108,13 +144,13 @@ template <class R> __device__ __forceinline__ void add_scaled_vector(q4<R>& q, c
 // (applyPositionChange, contact.go:374-375): the increment 0.5 * (v q) in R
 // from q rounded to R, accumulated in W.  With R == W it is AddScaledVector.
 template <class R, class W> __device__ __forceinline__ void add_scaled_vector_island(q4<W>& q, const v3<R>& v) {
-  const q4<R> qr = cvtq<R>(q);
+  const q4<R> qr{cvt_fast<R>(q.w), cvt_fast<R>(q.x), cvt_fast<R>(q.y), cvt_fast<R>(q.z)};
   q4<R> t{(R)0, v.x * (R)1, v.y * (R)1, v.z * (R)1};
   t = qmul(t, qr);
-  q.w += (W)(t.w * (R)0.5);
-  q.x += (W)(t.x * (R)0.5);
-  q.y += (W)(t.y * (R)0.5);
-  q.z += (W)(t.z * (R)0.5);
+  q.w += cvt_fast<W>(t.w * (R)0.5);
+  q.x += cvt_fast<W>(t.x * (R)0.5);
+  q.y += cvt_fast<W>(t.y * (R)0.5);
+  q.z += cvt_fast<W>(t.z * (R)0.5);
 }
 // quaternion.go:77-99
 template <class R> __device__ __forceinline__ void qnormalize(q4<R>& q) {
@@ -127,6 +163,37 @@ template <class R> __device__ __forceinline__ void qnormalize(q4<R>& q) {
   if (len == Lim<R>::inf()) len = Lim<R>::max_value();
   R inv = (R)1 / len;
   q.w *= inv; q.x *= inv; q.y *= inv; q.z *= inv;
+}
+
+// Quaternion renormalisation in the precision form's float64 island (W =
+// double, R = float).  A frame or a position change moves a unit quaternion
+// a little, so s = |q|^2 is near 1; with e = s - 1:
+//   |e| < 4e-7       nothing, where the reference's RealEqual(1, |q|) holds
+//                    (|1 - |q|| < 1e-7 (1 + |q|), and |q| - 1 is e/2 to first
+//                    order);
+//   |e| < 2^-11      q times 1/sqrt(s) from its Taylor series in e, five
+//                    terms by Horner (truncation below 1e-17): IEEE multiplies
+//                    and adds only, eight dependent float64 operations instead
+//                    of a square root and two divisions (about 30 dependent
+//                    ones at ~100 cycles each on GB300);
+//   otherwise        Normalize (quaternion.go:77-99) as the reference does.
+// The oracle's island evaluates the same operations.  With R == W (the plain
+// form) it is Normalize.
+template <class R, class W> __device__ __forceinline__ void qnormalize_island(q4<W>& q) {
+  if constexpr (sizeof(R) == sizeof(W)) {
+    qnormalize(q);
+  } else {
+    const W s = q.w * q.w + q.x * q.x + q.y * q.y + q.z * q.z;
+    const W e = s - (W)1;
+    const W ae = fabs(e);
+    if (ae < (W)4e-7) return;
+    if (ae < (W)0x1p-11) {
+      const W inv = (W)1 + e * ((W)-0.5 + e * ((W)0.375 + e * ((W)-0.3125 + e * (W)0.2734375)));
+      q.w *= inv; q.x *= inv; q.y *= inv; q.z *= inv;
+      return;
+    }
+    qnormalize(q);
+  }
 }
 
 // matrix.go:79-86

@@ -209,12 +209,12 @@ __device__ void prepare_contact(const RCtx<R, W>& x, const BatchView<R>& v, long
   if (stores_tangent<R>()) x.setCv(W_TYX, k, contact_tangent(n));  // calculateContactBasis
   const m3<R> C = x.basis(k);
   v3<R> rp0 = p;
-  sub(rp0, V<R>((R)x.P(0, b0), (R)x.P(1, b0), (R)x.P(2, b0)));
+  sub(rp0, V<R>((R)(x.P(0, b0)), (R)(x.P(1, b0)), (R)(x.P(2, b0))));
   v3<R> cv = local_velocity(x, b0, rp0, C);
   v3<R> rp1 = V<R>((R)0, (R)0, (R)0);
   if (b1 >= 0) {
     rp1 = p;
-    sub(rp1, V<R>((R)x.P(0, b1), (R)x.P(1, b1), (R)x.P(2, b1)));
+    sub(rp1, V<R>((R)(x.P(0, b1)), (R)(x.P(1, b1)), (R)(x.P(2, b1))));
     v3<R> cv1 = local_velocity(x, b1, rp1, C);
     sub(cv, cv1);
   }
@@ -243,7 +243,7 @@ template <class R, class W>
 __device__ void derive_asleep(const RCtx<R, W>& x, const BatchView<R>& v, int bstart, int body) {
   q4<R> q{(R)x.P(3, body), (R)x.P(4, body), (R)x.P(5, body), (R)x.P(6, body)};
   q4<W> qw = cvtq<W>(q);
-  qnormalize(qw);
+  qnormalize_island<R, W>(qw);
   q = cvtq<R>(qw);
   R rm[9];
   rotation_of(q, rm);
@@ -316,12 +316,12 @@ __device__ void apply_position_change(const RCtx<R, W>& x, const BatchView<R>& v
     lin = n;
     mul_with(lin, lm);
     // Position.AddScaled(normal, linearMove): product in R, accumulated in W
-    x.P(0, b) += (W)(n.x * lm);
-    x.P(1, b) += (W)(n.y * lm);
-    x.P(2, b) += (W)(n.z * lm);
+    x.P(0, b) += cvt_fast<W>(n.x * lm);
+    x.P(1, b) += cvt_fast<W>(n.y * lm);
+    x.P(2, b) += cvt_fast<W>(n.z * lm);
     q4<W> q{x.P(3, b), x.P(4, b), x.P(5, b), x.P(6, b)};
     add_scaled_vector_island<R, W>(q, ang);
-    qnormalize(q);
+    qnormalize_island<R, W>(q);
     x.P(3, b) = q.w; x.P(4, b) = q.x; x.P(5, b) = q.y; x.P(6, b) = q.z;
     if (!x.aw[b]) {
       // CalculateDerivedData reads the stored (R-rounded) orientation
@@ -383,10 +383,10 @@ template <class R, class W> __device__ __forceinline__ void friction_prepare(con
   const m3<R> dv = friction_response(x, k, body0_of(bb), body1_of(bb), x.basis(k));
   m3<W> dv_w;
 #pragma unroll
-  for (int q = 0; q < 9; ++q) dv_w.m[q] = (W)dv.m[q];
+  for (int q = 0; q < 9; ++q) dv_w.m[q] = (W)(dv.m[q]);
   const m3<W> K = invert(dv_w);
 #pragma unroll
-  for (int q = 0; q < 9; ++q) x.K(q, k) = (R)K.m[q];
+  for (int q = 0; q < 9; ++q) x.K(q, k) = (R)(K.m[q]);
   x.KD(0, k) = dv.m[0];
   x.KD(1, k) = dv.m[3];
   x.KD(2, k) = dv.m[6];
@@ -471,13 +471,13 @@ __device__ __forceinline__ void load_bodies(const RCtx<R, W>& x, const BatchView
   const long long S = v.nb_pad;
   for (int i = first; i < n; i += step) {
     const long long g = bstart + i;
-    x.P(0, i) = (W)v.body[B_PX * S + g];
-    x.P(1, i) = (W)v.body[B_PY * S + g];
-    x.P(2, i) = (W)v.body[B_PZ * S + g];
-    x.P(3, i) = (W)v.body[B_QW * S + g];
-    x.P(4, i) = (W)v.body[B_QX * S + g];
-    x.P(5, i) = (W)v.body[B_QY * S + g];
-    x.P(6, i) = (W)v.body[B_QZ * S + g];
+    x.P(0, i) = (W)(v.body[B_PX * S + g]);
+    x.P(1, i) = (W)(v.body[B_PY * S + g]);
+    x.P(2, i) = (W)(v.body[B_PZ * S + g]);
+    x.P(3, i) = (W)(v.body[B_QW * S + g]);
+    x.P(4, i) = (W)(v.body[B_QX * S + g]);
+    x.P(5, i) = (W)(v.body[B_QY * S + g]);
+    x.P(6, i) = (W)(v.body[B_QZ * S + g]);
 #pragma unroll
     for (int r = 0; r < 3; ++r) {
       x.Bf(r, i) = v.body[(B_VX + r) * S + g];
@@ -1214,13 +1214,13 @@ __global__ void __launch_bounds__(32, LEARN ? (G == 32 && sizeof(R) == 4 ? 18 : 
     if (active) {
       for (int i = gl; i < n; i += G) {
         const long long g = bstart + i;
-        v.body[B_PX * S + g] = (R)x.P(0, i);
-        v.body[B_PY * S + g] = (R)x.P(1, i);
-        v.body[B_PZ * S + g] = (R)x.P(2, i);
-        v.body[B_QW * S + g] = (R)x.P(3, i);
-        v.body[B_QX * S + g] = (R)x.P(4, i);
-        v.body[B_QY * S + g] = (R)x.P(5, i);
-        v.body[B_QZ * S + g] = (R)x.P(6, i);
+        v.body[B_PX * S + g] = (R)(x.P(0, i));
+        v.body[B_PY * S + g] = (R)(x.P(1, i));
+        v.body[B_PZ * S + g] = (R)(x.P(2, i));
+        v.body[B_QW * S + g] = (R)(x.P(3, i));
+        v.body[B_QX * S + g] = (R)(x.P(4, i));
+        v.body[B_QY * S + g] = (R)(x.P(5, i));
+        v.body[B_QZ * S + g] = (R)(x.P(6, i));
 #pragma unroll
         for (int r = 0; r < 3; ++r) {
           v.body[(B_VX + r) * S + g] = x.Bf(r, i);

@@ -94,7 +94,7 @@ __global__ void k_static_in(unsigned char* scratch, cz_bodies in, const cz_conta
       for (int k = 0; k < 9; ++k) iw.m[k] = (R)in.inverse_inertia_world[9 * i + k];
     } else {
       cz::q4<W> qw = cz::cvtq<W>(q);
-      cz::qnormalize(qw);
+      cz::qnormalize_island<R, W>(qw);
       q = cz::cvtq<R>(qw);
       R rm[9];
       cz::rotation_of(q, rm);

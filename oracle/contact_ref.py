@@ -139,6 +139,23 @@ def quat_add_scaled_vector(q, v, scale):  # quaternion.go:20-33
         q[k] += inc[k]
 
 
+def quat_normalize_island(q):
+    """The precision form's float64 renormalisation of q (a list of floats):
+    with s = |q|^2 and e = s - 1, nothing when |e| < 4e-7 (where
+    RealEqual(1, |q|) holds), q * 1/sqrt(s) from its five-term Taylor series
+    in e when |e| < 2^-11, else Normalize."""
+    s = q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + q[3] * q[3]
+    e = s - 1.0
+    if abs(e) < 4e-7:
+        return
+    if abs(e) < 2.0 ** -11:
+        inv = 1.0 + e * (-0.5 + e * (0.375 + e * (-0.3125 + e * 0.2734375)))
+        for i in range(4):
+            q[i] *= inv
+        return
+    quat_normalize(q)
+
+
 def quat_normalize(q):  # quaternion.go:78-99
     length = math.sqrt(q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + q[3] * q[3])
     if real_equal(1.0, length):
@@ -294,7 +311,10 @@ def _apply_position_change(c, bodies, penetration):  # contact.go:286-386
             inc = quat_scaled_increment([t(x) for x in qw], ang_change[i], t(1.0))
             for k in range(4):
                 qw[k] += float(inc[k])
-        quat_normalize(qw)
+        if t is float:
+            quat_normalize(qw)
+        else:
+            quat_normalize_island(qw)
         b["position"] = [t(x) for x in pw]
         b["orientation"] = [t(x) for x in qw]
         if not b["awake"]:

@@ -384,10 +384,33 @@ template <class R> inline void transformInertiaTensor(M3<R>& w, const M3<R>& b, 
   w[8] = t52 * r[2] + t57 * r[5] + t62 * r[8];
 }
 
+// Quaternion renormalisation of an orientation held in W (quaternion.go:
+// 77-99).  The plain form (R == W) is Normalize.  The precision form's
+// float64 island: with s = |q|^2 and e = s - 1, nothing when |e| < 4e-7
+// (where RealEqual(1, |q|) holds), q * 1/sqrt(s) from its five-term Taylor
+// series in e when |e| < 2^-11 (IEEE multiplies and adds only), else
+// Normalize.
+template <class R, class W> inline void NormalizeW(Q4<W>& q) {
+  if (sizeof(R) == sizeof(W)) {
+    Normalize(q);
+    return;
+  }
+  const W s = q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + q[3] * q[3];
+  const W e = s - (W)1;
+  const W ae = e < (W)0 ? -e : e;
+  if (ae < (W)4e-7) return;
+  if (ae < (W)0x1p-11) {
+    const W inv = (W)1 + e * ((W)-0.5 + e * ((W)0.375 + e * ((W)-0.3125 + e * (W)0.2734375)));
+    q[0] *= inv; q[1] *= inv; q[2] *= inv; q[3] *= inv;
+    return;
+  }
+  Normalize(q);
+}
+
 // Quaternion renormalisation, in W (rigidbody.go:269 -> quaternion.go:78-99)
 template <class R, class W> inline void NormalizeIsland(Q4<R>& q) {
   Q4<W> qw = cq4<W>(q);
-  Normalize(qw);
+  NormalizeW<R, W>(qw);
   q = cq4<R>(qw);
 }
 
@@ -964,7 +987,7 @@ template <class R, class W> struct Resolver {
       // the increment in R from the orientation rounded to R, accumulated in W
       Q4<W>& qw = oriW[c.body[i]];
       AddScaledVectorIsland<R, W>(qw, angularChange[i]);
-      Normalize(qw);
+      NormalizeW<R, W>(qw);
       body.position = cv3<R>(pw);
       body.orientation = cq4<R>(qw);
       if (body.isAwake == false) {

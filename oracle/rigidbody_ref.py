@@ -16,6 +16,7 @@ import math
 
 from oracle import colliders_ref, contact_ref
 from oracle.contact_ref import (add_scaled, dot, m3_mul_vector, mul_with, quat_add_scaled_vector, quat_normalize,
+                                quat_normalize_island,
                                 real_type)
 
 SLEEP_EPSILON = 0.3  # rigidbody.go:14 (an untyped constant: 10 * it is exactly 3)
@@ -49,7 +50,10 @@ def calculate_derived_data(b):  # rigidbody.go:268-272
     q = b["orientation"]
     rt = real_type(*q)
     qw = [float(x) for x in q]  # the renormalisation in float64
-    quat_normalize(qw)
+    if rt is float:
+        quat_normalize(qw)
+    else:
+        quat_normalize_island(qw)
     b["orientation"] = [rt(x) for x in qw]
     t = colliders_ref.set_as_transform(b["position"], b["orientation"])
     b["iit"] = transform_inertia_tensor(b["iit_body"], t)
