@@ -54,6 +54,12 @@ METRIC = "body-steps/s: FP32+MLP warm-start vs plain FP64 on 1 GB300 at stated e
 UNIT = "body-steps/s"
 DT = 1.0 / 60.0
 L2_BYTES = 126 * 1024 * 1024
+# DRAM bytes (read + write) of one resolver launch at steady state on the
+# default workload (16384 worlds x 32 bodies), from an ncu capture of the
+# resolver instantiation the headline form runs (frame 381 of a 400-frame
+# rollout): the roofline's measured traffic beside its algorithmic bytes.
+RESOLVE_TRAFFIC = {"bytes": 186.1e6, "kernel": "k_resolve<float, double, 32, false>",
+                   "source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, one launch"}
 
 
 def _peaks():
@@ -320,6 +326,7 @@ def run_ours(args):
 
     r32 = results[head]
     real = 4 if batches[head].form == FORM_FP32 else 8
+    default_size = args.worlds == 16384 and args.bodies == 32 and real == 4
     phase_names = ["integrate", "narrowphase", "resolve"]
     ph = r32["phase_ms"]
     dom = int(np.argmax(ph))
@@ -385,7 +392,9 @@ def run_ours(args):
         "gpu_launches": r32["launches"],
         "clocks": r32["clocks"],
         "roofline": {"kernel": phase_names[dom], "bound": "hbm", "achieved": achieved, "peak": peak,
-                     "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind, "traffic": None,
+                     "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
+                     "traffic": RESOLVE_TRAFFIC["bytes"] if default_size and dom == 2 else None,
+                     "traffic_source": dict(RESOLVE_TRAFFIC, bytes=None) if default_size and dom == 2 else None,
                      "note": "the resolver is sequential per world and latency / float64-pipe bound; its HBM "
                              "fraction is reported as asked, iterations per second below"},
         "resolver_iterations_per_s": (cnt["pos_iterations"] + cnt["vel_iterations"]) / (args.steps * ph[2] / 1e3),
