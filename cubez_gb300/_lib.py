@@ -46,7 +46,7 @@ class Tuning(C.Structure):
     _fields_ = [("narrowphase_threads", C.c_int32), ("resolver_contacts", C.c_int32),
                 ("resolver_ctas_per_sm", C.c_int32), ("integrate_threads", C.c_int32), ("resolver_lanes", C.c_int32),
                 ("warm_start_budget_shift", C.c_int32), ("large_world_lanes", C.c_int32),
-                ("broadphase_min_bodies", C.c_int32)]
+                ("broadphase_min_bodies", C.c_int32), ("fused_frame", C.c_int32)]
 
 
 # every symbol include/cubez_gpu.h declares, with (restype, argtypes)

@@ -6,6 +6,8 @@ Searches, on the caller's own batch and scene state, over
   * the narrowphase CTA size,
   * with worlds of more than 64 bodies in the batch, the large-world
     resolver's lanes per world (32, or 16 = two worlds per warp),
+  * with one world per warp, the fused frame (one launch per frame) or the
+    three launches (it compares whole frames: the fused frame has no phases),
   * with the learned warm start enabled, optionally the warm-start budget
     threshold (which worlds are warm-started; it changes which of two valid
     solutions a world gets, within the resolver's epsilon, and the speed),
@@ -29,7 +31,7 @@ BIG_WORLD = 64  # worlds of more bodies than this go to the large-world resolver
 
 
 def tune(batch, frames=30, dt=1.0 / 60.0, lanes=DEFAULT_LANES, tiles=DEFAULT_TILES, np_threads=DEFAULT_NP_THREADS,
-         warm_shifts=(), large_lanes=DEFAULT_LARGE_LANES, repeats=1, log=None):
+         warm_shifts=(), large_lanes=DEFAULT_LARGE_LANES, fused=True, repeats=1, log=None):
     """Returns (best_config, trials); the batch is left at best_config."""
     trials = []
 
@@ -66,6 +68,17 @@ def tune(batch, frames=30, dt=1.0 / 60.0, lanes=DEFAULT_LANES, tiles=DEFAULT_TIL
         if best_ms is None or ph[2] < best_ms:
             best, best_ms = (g, cfg["resolver_contacts"]), ph[2]
     batch.set_tuning(resolver_lanes=best[0], resolver_contacts=best[1])
+    # one launch per frame, where the batch allows it (one world per warp, no
+    # world above the slot, the plain resolver): the batch ignores it otherwise
+    if fused and best[0] == 32 and not (np.asarray(batch.counts) > BIG_WORLD).any():
+        best_f, f_ms = None, None
+        for f in (-1, 1):
+            batch.set_tuning(fused_frame=f)
+            ph = measure()
+            trials.append({"fused_frame": f, "step_ms": float(ph.sum())})
+            if f_ms is None or ph.sum() < f_ms:
+                best_f, f_ms = f, ph.sum()
+        batch.set_tuning(fused_frame=best_f)
     if large_lanes and (np.asarray(batch.counts) > BIG_WORLD).any():
         best_ll, ll_ms = None, None
         for g in large_lanes:

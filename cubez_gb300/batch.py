@@ -203,9 +203,10 @@ class WorldBatch:
 
     # ---------------------------------------------------------------- tuning
     def set_tuning(self, narrowphase_threads=0, resolver_contacts=0, resolver_ctas_per_sm=0, integrate_threads=0,
-                   resolver_lanes=0, warm_start_budget_shift=0, large_world_lanes=0, broadphase_min_bodies=0):
+                   resolver_lanes=0, warm_start_budget_shift=0, large_world_lanes=0, broadphase_min_bodies=0,
+                   fused_frame=0):
         t = _lib.Tuning(narrowphase_threads, resolver_contacts, resolver_ctas_per_sm, integrate_threads, resolver_lanes,
-                        warm_start_budget_shift, large_world_lanes, broadphase_min_bodies)
+                        warm_start_budget_shift, large_world_lanes, broadphase_min_bodies, fused_frame)
         check(self.L.cz_set_tuning(self.h, C.byref(t)))
 
     def get_tuning(self):
@@ -214,4 +215,5 @@ class WorldBatch:
         return {"narrowphase_threads": t.narrowphase_threads, "resolver_contacts": t.resolver_contacts,
                 "resolver_ctas_per_sm": t.resolver_ctas_per_sm, "integrate_threads": t.integrate_threads,
                 "resolver_lanes": t.resolver_lanes, "warm_start_budget_shift": t.warm_start_budget_shift,
-                "large_world_lanes": t.large_world_lanes, "broadphase_min_bodies": t.broadphase_min_bodies}
+                "large_world_lanes": t.large_world_lanes, "broadphase_min_bodies": t.broadphase_min_bodies,
+                "fused_frame": t.fused_frame}

@@ -130,6 +130,9 @@ struct cz_batch {
   int wait_limit = 1 << 22;  // polls of the narrowphase's bounded wait
   int wait_extra_tx = 0;     // test hook: bytes that wait expects beyond its copies
   int grid_min_bodies = 128; // narrowphase grid for worlds of at least this many bodies (0: never)
+  int fused = 0;             // one launch per frame (the fused frame) where the batch allows it
+  size_t fr_smem = 0;        // the fused frame's shared memory per CTA (0: it does not fit)
+  int fr_grid = 1;           // the fused frame's CTAs
   int mode = 0;      // resolver mode: 0 plain, 1 harvest, 2 learned warm start
   cz::MlpDev mlp{};  // device copy of the warm-start network
   void* mlp_mem = nullptr;
@@ -337,7 +340,14 @@ int ensure_pows(cz_batch* b, double dt) {
   return CZ_OK;
 }
 
+// Whether stepping runs the fused frame: one world per warp, plain resolver,
+// every world within the shared-memory slot.
+bool uses_frame(const cz_batch* b) {
+  return b->fused && b->fr_smem > 0 && b->big_ids.empty() && b->rs_lanes == 32 && b->mode == 0 && b->nsmall > 0;
+}
+
 int launches_per_step(const cz_batch* b) {
+  if (uses_frame(b)) return 1 + (b->nsmall > 1 ? 1 : 0);
   return 2 + (b->nsmall > 0 ? 1 + (b->nsmall > 32 / b->rs_lanes ? 1 : 0) + (b->mode != 0 ? 1 : 0) : 0) +
          (b->big_ids.empty() ? 0 : 1);
 }
@@ -381,6 +391,19 @@ int launch_resolve_with(cz_batch* b, double dt, const cz::HostView& v, int cs, s
 int launch_resolve(cz_batch* b, double dt, const cz::HostView* override_view = nullptr) {
   return launch_resolve_with(b, dt, override_view ? *override_view : b->view(), b->rs_cs, b->rs_smem);
 }
+// The fused frame: integrate, narrowphase and resolve of every world in one
+// launch (then the re-queue by cost).
+int launch_frame(cz_batch* b, double dt) {
+  CZ_CUDA(cudaMemsetAsync(b->d_queue + 1, 0, sizeof(unsigned), b->stream));
+  CZ_CUDA(b->ops->frame(b->view(), b->rs_nbs, b->rs_cs, b->fr_grid, b->fr_smem, dt, std::pow(0.5, dt), b->stream));
+  g_launches++;
+  if (b->nsmall > 1) {
+    k_reorder<<<1, 1024, 0, b->stream>>>(b->d_piters, b->d_viters, b->num_worlds, b->d_order_rs);
+    CZ_CUDA(cudaGetLastError());
+    g_launches++;
+  }
+  return CZ_OK;
+}
 
 // The captured graphs hold the kernels' parameters (the batch view); drop them
 // whenever those change.
@@ -418,6 +441,17 @@ int configure(cz_batch* b) {
   b->rs_grid = std::max(b->rs_grid, 1);
   b->wf_grid = (int)std::min<long long>(std::max(b->nsmall, 1),
                                         (long long)b->ops->warm_features_blocks(b->rs_nbs) * b->sm_count);
+  // the fused frame's slot holds the resolver's tile and the narrowphase's
+  b->fr_smem = b->ops->frame_smem(b->rs_nbs, b->rs_cs);
+  if (b->fr_smem > b->smem_optin) {
+    b->fr_smem = 0;
+  } else {
+    int frb = 0;
+    CZ_CUDA(b->ops->frame_occupancy(&frb, b->fr_smem));
+    frb = std::max(frb, 1);
+    if (b->rs_ctas_per_sm > 0) frb = std::min(frb, b->rs_ctas_per_sm);
+    b->fr_grid = (int)std::max<long long>(1, std::min<long long>(std::max(b->nsmall, 1), (long long)frb * b->sm_count));
+  }
   drop_graphs(b);
   return CZ_OK;
 }
@@ -633,6 +667,7 @@ int cz_set_tuning(cz_batch* b, const cz_tuning* t) {
     if (t->warm_start_budget_shift > 8) return fail(CZ_ERR_BAD_ARG, "warm_start_budget_shift must be 1 to 8");
     b->warm_shift = t->warm_start_budget_shift;
   }
+  if (t->fused_frame != 0) b->fused = t->fused_frame > 0 ? 1 : 0;
   if (t->broadphase_min_bodies != 0) {
     if (t->broadphase_min_bodies < -1) return fail(CZ_ERR_BAD_ARG, "broadphase_min_bodies must be -1 or positive");
     b->grid_min_bodies = t->broadphase_min_bodies < 0 ? 0 : t->broadphase_min_bodies;
@@ -657,6 +692,7 @@ int cz_get_tuning(cz_batch* b, cz_tuning* t) {
   t->resolver_lanes = b->rs_lanes;
   t->warm_start_budget_shift = b->warm_shift;
   t->broadphase_min_bodies = b->grid_min_bodies > 0 ? b->grid_min_bodies : -1;
+  t->fused_frame = b->fused ? 1 : -1;
   t->large_world_lanes = b->big_lanes;
   return CZ_OK;
 }
@@ -817,7 +853,12 @@ static int get_graph(cz_batch* b, int nsteps, double dt, cudaGraphExec_t* out) {
   CZ_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
   const long long before = g_launches.load();
   int cst = CZ_OK;
+  const bool fused = uses_frame(b);
   for (int s = 0; s < nsteps && cst == CZ_OK; ++s) {
+    if (fused) {
+      cst = launch_frame(b, dt);
+      continue;
+    }
     cst = launch_integrate(b, dt);
     if (!cst) cst = launch_narrowphase(b);
     if (!cst) cst = launch_resolve(b, dt);
@@ -857,7 +898,15 @@ static int get_timed(cz_batch* b, int nsteps, double dt, cz_batch::Timed** out) 
                                                                                                 : CZ_ERR_CUDA;
   };
   int cst = record(0);
+  const bool fused = uses_frame(b);
   for (int s = 0; s < nsteps && cst == CZ_OK; ++s) {
+    if (fused) {  // one launch: its time is reported as the resolve phase
+      cst = record(3 * s + 1);
+      if (!cst) cst = record(3 * s + 2);
+      if (!cst) cst = launch_frame(b, dt);
+      if (!cst) cst = record(3 * s + 3);
+      continue;
+    }
     cst = launch_integrate(b, dt);
     if (!cst) cst = record(3 * s + 1);
     if (!cst) cst = launch_narrowphase(b);

@@ -272,6 +272,20 @@ static cudaError_t resolve(const HostView& h, int nbs, int cs, int lanes, int gr
   return cudaGetLastError();
 }
 
+static size_t frame_smem(int nbs, int cs) { return frame_slot_bytes<R, W>(nbs, cs); }
+
+static cudaError_t frame_occupancy(int* blocks, size_t smem) {
+  cudaError_t e = raise_smem_limit((const void*)k_resolve<R, W, 32, false, true>, smem);
+  if (e != cudaSuccess) return e;
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, k_resolve<R, W, 32, false, true>, 32, smem);
+}
+
+static cudaError_t frame(const HostView& h, int nbs, int cs, int grid, size_t smem, double dt, double sleep_bias,
+                         cudaStream_t s) {
+  k_resolve<R, W, 32, false, true><<<grid, 32, smem, s>>>(view_of(h), nbs, cs, (R)dt, (R)sleep_bias);
+  return cudaGetLastError();
+}
+
 static cudaError_t collide(const HostView& h, int world, const void* units, int nunits, int nbs, size_t smem,
                            cudaStream_t s) {
   const void* f = (const void*)k_collide<R>;
@@ -386,6 +400,9 @@ const FormOps CZ_FORM_OBJ = {sizeof(CZ_R),
                              CZ_FORM_NS::contacts_out,
                              CZ_FORM_NS::contacts_in,
                              CZ_FORM_NS::set_rows,
-                             CZ_FORM_NS::resolve_fn};
+                             CZ_FORM_NS::resolve_fn,
+                             CZ_FORM_NS::frame_smem,
+                             CZ_FORM_NS::frame,
+                             CZ_FORM_NS::frame_occupancy};
 
 }  // namespace cz

@@ -110,6 +110,11 @@ struct FormOps {
                              cudaStream_t s);
   cudaError_t (*set_rows)(const HostView& v, int row, int nrows, const double* src, cudaStream_t s);
   const void* (*resolve_kernel)(int lanes);  // the resolver instantiation for `lanes` lanes per world
+  // the fused frame (k_frame): integrate, narrowphase and resolver per world, one warp each
+  size_t (*frame_smem)(int nbs, int cs);
+  cudaError_t (*frame)(const HostView& v, int nbs, int cs, int grid, size_t smem, double dt, double sleep_bias,
+                       cudaStream_t s);
+  cudaError_t (*frame_occupancy)(int* blocks, size_t smem);  // also raises its shared-memory limit
 };
 
 extern const FormOps kFormFP64;

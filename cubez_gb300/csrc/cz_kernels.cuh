@@ -23,10 +23,10 @@ constexpr unsigned FULL = 0xffffffffu;
 
 // ============================================================== integrate
 
+// RigidBody.Integrate + CalculateDerivedData of body row i
+// (rigidbody.go:213-299), in place in the batch rows.
 template <class R, class W>
-__global__ void __launch_bounds__(256) k_integrate(BatchView<R> v, R dt, R sleep_bias) {
-  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= v.nb_pad) return;
+__device__ __forceinline__ void integrate_body(const BatchView<R>& v, long long i, R dt, R sleep_bias) {
   if (!v.awake[i]) return;  // rigidbody.go:214-216
   const long long S = v.nb_pad;
   R* b = v.body + i;
@@ -82,6 +82,13 @@ __global__ void __launch_bounds__(256) k_integrate(BatchView<R> v, R dt, R sleep
 #pragma unroll
   for (int k = 0; k < 9; ++k) F(B_IW0 + k) = iw.m[k];
 #undef F
+}
+
+template <class R, class W>
+__global__ void __launch_bounds__(256) k_integrate(BatchView<R> v, R dt, R sleep_bias) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= v.nb_pad) return;
+  integrate_body<R, W>(v, i, dt, sleep_bias);
 }
 
 // ============================================================== narrowphase
@@ -830,6 +837,92 @@ __device__ int np_grid_units(const NPTile<R>& tl, const BatchView<R>& v, const N
   return cnt;
 }
 
+// The narrowphase of world w, its bodies' tile built: the ordered units
+// culled, the kept ones listed (scap of them at a time) and tested, the
+// contacts emitted in the reference's order; sets the world's contact count.
+// Every thread of the CTA calls it.
+template <class R, bool GRID>
+__device__ void np_world(const NPTile<R>& tl, const BatchView<R>& v, int w, int n, int bstart, int* scan,
+                         int& chunk_parity, int* surv, int scap) {
+  const int tid = threadIdx.x;
+  const long long cs = v.contact_start[w];
+  const int cap = v.contact_cap[w];
+  const int U = n * n;  // ordered units: for body i, the half-space (k = 0), then k - 1 = j skipping i
+  int out = 0, nsurv = 0;
+  uint32_t err = 0;
+  const NPGrid g = np_grid_scratch(tl);
+  if (GRID && v.grid_min_bodies > 0 && n >= v.grid_min_bodies && np_grid_build(tl, n, g, scan, chunk_parity)) {
+    // Grid: each body's kept units (counted, then listed and sorted), as
+    // many bodies at a time as the list holds, then their full tests.
+    for (int ib = 0; ib < n;) {
+      const int i = ib + tid;
+      const int cnt = i < n ? np_grid_units(tl, v, g, n, i, nullptr) : 0;
+      int excl, total;
+      np_chunk_scan(cnt, scan, chunk_parity, &excl, &total);
+      chunk_parity ^= 1;
+      const bool fits = i < n && excl + cnt <= scap;  // a prefix of the bodies: at least body ib
+      const int m = __syncthreads_count(fits);
+      if (fits) {
+        int* d = surv + excl;
+        np_grid_units(tl, v, g, n, i, d);
+        for (int a = 1; a < cnt; ++a) {  // ascending unit order (the plane unit, k = 0, first)
+          const int key = d[a];
+          int b = a - 1;
+          while (b >= 0 && d[b] > key) {
+            d[b + 1] = d[b];
+            --b;
+          }
+          d[b + 1] = key;
+        }
+        if (tid == m - 1) g.info[5] = excl + cnt;
+      }
+      __syncthreads();
+      nsurv = g.info[5];
+      np_flush(tl, v, bstart, n, cs, cap, surv, nsurv, scan, chunk_parity, out, err);
+      __syncthreads();
+      ib += m;
+    }
+  } else {
+    // All pairs: the culls run over every unit; the units they keep are
+    // listed in unit order and get their full tests in chunks of the CTA's
+    // size, so the lanes of a warp run the costly tests together.
+    // Counting, scanning and emitting in list order keeps the reference's
+    // contact order.
+    for (int base = 0; base < U; base += blockDim.x) {
+      const int u = base + tid;
+      bool keep = false;
+      if (u < U) {
+        const int i = u / n, k = u - i * n;
+        int j = k - 1;
+        if (j >= i) ++j;
+        keep = k == 0 ? !plane_culled(tl, i, v) : !pair_culled(tl, i, j);
+      }
+      int excl, total;
+      np_chunk_scan(keep ? 1 : 0, scan, chunk_parity, &excl, &total);
+      chunk_parity ^= 1;
+      if (keep) surv[nsurv + excl] = u;
+      nsurv += total;
+      if (nsurv <= scap - (int)blockDim.x && base + (int)blockDim.x < U) continue;
+      __syncthreads();
+      np_flush(tl, v, bstart, n, cs, cap, surv, nsurv, scan, chunk_parity, out, err);
+      nsurv = 0;
+      __syncthreads();
+    }
+  }
+  if (err) {
+    atomicOr(&v.world_status[w], err);
+    atomicOr(v.status, err);
+  }
+  if (tid == 0) {
+    v.contact_count[w] = out;
+    atomicAdd(&v.counters[0], (unsigned long long)out);
+    if (out > cap) {
+      atomicOr(&v.world_status[w], ST_CAPACITY);
+      atomicOr(v.status, ST_CAPACITY);
+    }
+  }
+}
+
 // GRID = false compiles the all-pairs path alone (worlds too small for the
 // grid), so its registers and occupancy stay those of that path.
 template <class R, bool GRID>
@@ -902,83 +995,7 @@ __global__ void __launch_bounds__(256) k_narrowphase(BatchView<R> v, int nbs) {
     }
     np_build_tile(tl, n, v.offset ? v.offset + bstart : nullptr, v.nb_pad);
     __syncthreads();
-    const long long cs = v.contact_start[w];
-    const int cap = v.contact_cap[w];
-    const int U = n * n;  // ordered units: for body i, the half-space (k = 0), then k - 1 = j skipping i
-    const int scap = np_surv_cap(nbs);
-    int out = 0, nsurv = 0;
-    uint32_t err = 0;
-    const NPGrid g = np_grid_scratch(tl);
-    if (GRID && v.grid_min_bodies > 0 && n >= v.grid_min_bodies && np_grid_build(tl, n, g, scan, chunk_parity)) {
-      // Grid: each body's kept units (counted, then listed and sorted), as
-      // many bodies at a time as the list holds, then their full tests.
-      for (int ib = 0; ib < n;) {
-        const int i = ib + tid;
-        const int cnt = i < n ? np_grid_units(tl, v, g, n, i, nullptr) : 0;
-        int excl, total;
-        np_chunk_scan(cnt, scan, chunk_parity, &excl, &total);
-        chunk_parity ^= 1;
-        const bool fits = i < n && excl + cnt <= scap;  // a prefix of the bodies: at least body ib
-        const int m = __syncthreads_count(fits);
-        if (fits) {
-          int* d = surv + excl;
-          np_grid_units(tl, v, g, n, i, d);
-          for (int a = 1; a < cnt; ++a) {  // ascending unit order (the plane unit, k = 0, first)
-            const int key = d[a];
-            int b = a - 1;
-            while (b >= 0 && d[b] > key) {
-              d[b + 1] = d[b];
-              --b;
-            }
-            d[b + 1] = key;
-          }
-          if (tid == m - 1) g.info[5] = excl + cnt;
-        }
-        __syncthreads();
-        nsurv = g.info[5];
-        np_flush(tl, v, bstart, n, cs, cap, surv, nsurv, scan, chunk_parity, out, err);
-        __syncthreads();
-        ib += m;
-      }
-    } else {
-      // All pairs: the culls run over every unit; the units they keep are
-      // listed in unit order and get their full tests in chunks of the CTA's
-      // size, so the lanes of a warp run the costly tests together.
-      // Counting, scanning and emitting in list order keeps the reference's
-      // contact order.
-      for (int base = 0; base < U; base += blockDim.x) {
-        const int u = base + tid;
-        bool keep = false;
-        if (u < U) {
-          const int i = u / n, k = u - i * n;
-          int j = k - 1;
-          if (j >= i) ++j;
-          keep = k == 0 ? !plane_culled(tl, i, v) : !pair_culled(tl, i, j);
-        }
-        int excl, total;
-        np_chunk_scan(keep ? 1 : 0, scan, chunk_parity, &excl, &total);
-        chunk_parity ^= 1;
-        if (keep) surv[nsurv + excl] = u;
-        nsurv += total;
-        if (nsurv <= scap - (int)blockDim.x && base + (int)blockDim.x < U) continue;
-        __syncthreads();
-        np_flush(tl, v, bstart, n, cs, cap, surv, nsurv, scan, chunk_parity, out, err);
-        nsurv = 0;
-        __syncthreads();
-      }
-    }
-    if (err) {
-      atomicOr(&v.world_status[w], err);
-      atomicOr(v.status, err);
-    }
-    if (tid == 0) {
-      v.contact_count[w] = out;
-      atomicAdd(&v.counters[0], (unsigned long long)out);
-      if (out > cap) {
-        atomicOr(&v.world_status[w], ST_CAPACITY);
-        atomicOr(v.status, ST_CAPACITY);
-      }
-    }
+    np_world<R, GRID>(tl, v, w, n, bstart, scan, chunk_parity, surv, np_surv_cap(nbs));
     __syncthreads();
   }
 }

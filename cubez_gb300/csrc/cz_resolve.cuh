@@ -986,14 +986,70 @@ __device__ int velocity_loop_w(const RCtx<R, W>& x, const BatchView<R>& v, int w
 // k_warm_features' plan) with fallback to the plain solve.  LEARN = false
 // compiles the plain resolver alone (v.mode is ignored), so the learned paths
 // cost the plain kernel no registers.
-template <class R, class W, int G, bool LEARN>
-__global__ void __launch_bounds__(32, LEARN ? (G == 32 && sizeof(R) == 4 ? 18 : 16) : 0) k_resolve(BatchView<R> v, int nbs, int cs, R dt) {
-  constexpr int NG = 32 / G;
+// ---------------------------------------------------------------- one frame per world
+// Survivor list of the narrowphase inside the fused frame (one warp per CTA).
+constexpr int kFrameSurvivors = 128;
+
+// Bytes of the narrowphase tile of one world in the fused frame: staged rows
+// and collider transforms, shapes, cull data, scan scratch, survivor list.
+template <class R> __host__ __device__ inline size_t frame_tile_bytes(int nbs) {
+  size_t b = (size_t)(11 + 12) * nbs * sizeof(R) + (size_t)nbs * sizeof(int) + (size_t)5 * nbs * sizeof(float);
+  b += (66 + kFrameSurvivors) * sizeof(int);
+  return (b + 15) & ~(size_t)15;
+}
+// The fused frame's slot: the resolver's, large enough for the narrowphase
+// tile too (the narrowphase runs first, in the same bytes).
+template <class R, class W> __host__ __device__ inline size_t frame_slot_bytes(int nbs, int cs) {
+  const size_t a = rs_slot_bytes<R, W>(nbs, cs), b = frame_tile_bytes<R>(nbs);
+  return a > b ? a : b;
+}
+
+// Integrate + the colliders' derived data of world w's bodies, then its
+// narrowphase, by the calling warp, the tile in the shared memory at base:
+// the first two steps of the frame of examples/cubedrop.go:69-75, as
+// k_integrate and k_narrowphase run them.
+template <class R, class W>
+__device__ void frame_front(const BatchView<R>& v, int w, int n, int bstart, int nbs, R dt, R sleep_bias,
+                            unsigned char* base) {
+  const int lane = threadIdx.x;
+  for (int i = lane; i < n; i += 32) integrate_body<R, W>(v, (long long)bstart + i, dt, sleep_bias);
+  __syncwarp();
+  NPTile<R> tl;
+  tl.nbs = nbs;
+  tl.stage = reinterpret_cast<R*>(base);
+  tl.T = tl.stage + 11 * nbs;
+  tl.shape = reinterpret_cast<int*>(tl.T + 12 * nbs);
+  tl.cull = reinterpret_cast<float*>(tl.shape + nbs);
+  int* scan = reinterpret_cast<int*>(tl.cull + 5 * nbs);
+  int* surv = scan + 66;
+  for (int i = lane; i < n; i += 32) {
+#pragma unroll
+    for (int r = 0; r < 11; ++r) tl.stage[r * nbs + i] = v.body[(long long)r * v.nb_pad + bstart + i];
+    tl.shape[i] = v.shape[bstart + i];
+  }
+  __syncwarp();
+  np_build_tile(tl, n, v.offset ? v.offset + bstart : nullptr, v.nb_pad);
+  __syncwarp();
+  int parity = 0;
+  np_world<R, false>(tl, v, w, n, bstart, scan, parity, surv, kFrameSurvivors);
+  __syncwarp();
+}
+
+// The resolver: G lanes per world, worlds from the device queue.  FRAME (the
+// fused frame): each world's integrate and narrowphase first
+// (frame_front), so one launch runs a whole frame (one world per warp, plain
+// resolver).
+template <class R, class W, int G, bool LEARN, bool FRAME = false>
+__global__ void __launch_bounds__(32, FRAME ? (sizeof(R) == 4 ? 18 : 8)
+                                            : (LEARN ? (G == 32 && sizeof(R) == 4 ? 18 : 16) : 0))
+    k_resolve(BatchView<R> v, int nbs, int cs, R dt, R sleep_bias = (R)0) {
+  static_assert(!FRAME || (G == 32 && !LEARN), "the fused frame runs one world per warp, plain");
   extern __shared__ __align__(128) unsigned char smem[];
+  constexpr int NG = 32 / G;
   const int lane = threadIdx.x;
   const int grp = lane / G, gl = lane % G;
   const int mode = LEARN ? v.mode : 0;
-  const size_t slot_bytes = rs_slot_bytes<R, W>(nbs, cs);
+  const size_t slot_bytes = FRAME ? frame_slot_bytes<R, W>(nbs, cs) : rs_slot_bytes<R, W>(nbs, cs);
   Slot<R, W> sl = make_slot<R, W>(smem + (size_t)grp * slot_bytes, nbs, cs, dt);
   RCtx<R, W>& x = sl.x;
   const long long S = v.nb_pad;
@@ -1008,6 +1064,10 @@ __global__ void __launch_bounds__(32, LEARN ? (G == 32 && sizeof(R) == 4 ? 18 : 
     if (has && v.big_count > 0 && v.body_count[w] > nbs) has = false;  // a world of k_resolve_big
     const int n = has ? v.body_count[w] : 0;
     const int bstart = has ? v.body_start[w] : 0;
+    if constexpr (FRAME) {
+      if (has && n <= nbs) frame_front<R, W>(v, w, n, bstart, nbs, dt, sleep_bias, smem);
+      __syncwarp();
+    }
     int C = has ? v.contact_count[w] : 0;
     if (has) {
       const int cap = v.contact_cap[w];
@@ -1235,6 +1295,7 @@ __global__ void __launch_bounds__(32, LEARN ? (G == 32 && sizeof(R) == 4 ? 18 : 
     __syncwarp();
   }
 }
+
 
 // ---------------------------------------------------------------- k_warm_features
 // Shared-memory copy of the inference weights (fragment layouts of MlpDev).

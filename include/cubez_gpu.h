@@ -279,6 +279,11 @@ typedef struct cz_tuning {
                                     contact lists are the same bit for bit (an ordered all-pairs
                                     loop, examples/cubedrop.go:41-67, that the reference marks as
                                     O(n^2) at examples/cubedrop.go:54 and README.md:98-99) */
+  int32_t fused_frame;         /* 1: cz_step runs each frame as one launch in which a warp integrates,
+                                  tests and resolves one world after another from a device queue;
+                                  -1: three launches per frame (the default).  Taken where the batch
+                                  runs one world per warp (resolver_lanes 32), the plain resolver
+                                  and no world above 64 bodies; same results either way */
 } cz_tuning;
 int cz_set_tuning(cz_batch* batch, const cz_tuning* tuning);
 int cz_get_tuning(cz_batch* batch, cz_tuning* tuning);

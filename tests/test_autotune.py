@@ -11,7 +11,7 @@ class FakeBatch:
     def __init__(self, counts):
         self.counts = np.asarray(counts, np.int32)
         self.cfg = {"narrowphase_threads": 128, "resolver_contacts": 128, "resolver_lanes": 8,
-                    "large_world_lanes": 32, "warm_start_budget_shift": 2}
+                    "large_world_lanes": 32, "warm_start_budget_shift": 2, "fused_frame": -1}
         self.restores = 0
         self.calls = []
 
@@ -33,6 +33,8 @@ class FakeBatch:
         npm = {32: 1.0, 64: 2.0, 128: 3.0, 256: 4.0}[c["narrowphase_threads"]]
         rs = 10.0 + abs(c["resolver_lanes"] - 16) + abs(c["resolver_contacts"] - 96) / 32.0
         rs += 5.0 if c["large_world_lanes"] == 16 else 0.0
+        if c["fused_frame"] == 1 and c["resolver_lanes"] == 32:
+            return 8.0, np.array([0.0, 0.0, 8.0])
         ph = np.array([0.5, npm, rs])
         return float(ph.sum()), ph
 
@@ -53,3 +55,14 @@ def test_large_world_lanes_tried_only_with_large_worlds():
     tried = [t["large_world_lanes"] for t in trials if "large_world_lanes" in t]
     assert tried == list(autotune.DEFAULT_LARGE_LANES)
     assert cfg["large_world_lanes"] == 32
+
+
+def test_fused_frame_tried_with_one_world_per_warp():
+    b = FakeBatch([32] * 8)
+    cfg, trials = autotune.tune(b, frames=2, lanes=(32,))
+    tried = [t["fused_frame"] for t in trials if "fused_frame" in t]
+    assert tried == [-1, 1]
+    assert cfg["fused_frame"] == 1
+    b = FakeBatch([32, 80])
+    cfg, trials = autotune.tune(b, frames=2, lanes=(32,))
+    assert not any("fused_frame" in t for t in trials)  # a world above the slot
