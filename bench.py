@@ -55,11 +55,15 @@ UNIT = "body-steps/s"
 DT = 1.0 / 60.0
 L2_BYTES = 126 * 1024 * 1024
 # DRAM bytes (read + write) of one resolver launch at steady state on the
-# default workload (16384 worlds x 32 bodies), from an ncu capture of the
-# resolver instantiation the headline form runs (frame 381 of a 400-frame
+# default workload (16384 worlds x 32 bodies), per form, from an ncu capture
+# of the resolver instantiation that form runs (frame 381 of a 400-frame
 # rollout): the roofline's measured traffic beside its algorithmic bytes.
-RESOLVE_TRAFFIC = {"bytes": 186.1e6, "kernel": "k_resolve<float, double, 32, false>",
-                   "source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, one launch"}
+RESOLVE_TRAFFIC = {
+    "fp32": {"bytes": 186.1e6, "kernel": "k_resolve<float, double, 32, false>",
+             "source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, one launch"},
+    "fp32_mlp": {"bytes": 205.9e6, "kernel": "k_resolve<float, double, 32, true>",
+                 "source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, one launch"},
+}
 
 
 def _peaks():
@@ -329,20 +333,28 @@ def run_ours(args):
     default_size = args.worlds == 16384 and args.bodies == 32 and real == 4
     phase_names = ["integrate", "narrowphase", "resolve"]
     ph = r32["phase_ms"]
+    # the fused frame (tuning fused_frame 1) reports its whole time as the resolve phase
+    fused = ph[0] == 0.0 and ph[1] == 0.0
+    if fused:
+        phase_names[2] = "frame"
     dom = int(np.argmax(ph))
     per_launch_ms = ph[dom] / frames
-    bytes_launch = _alg_bytes(dom, real, nb, r32["counters"], frames, args.steps)
+    alg = [_alg_bytes(i, real, nb, r32["counters"], frames, args.steps) for i in range(3)]
+    bytes_launch = sum(alg) if fused else alg[dom]
     peak, peak_kind = _peaks()
     achieved = bytes_launch / (per_launch_ms / 1e3) / 1e9
     kernels = {}
     for i, n in enumerate(phase_names):
-        bl = _alg_bytes(i, real, nb, r32["counters"], frames, args.steps)
+        if fused and i < 2:
+            continue
+        bl = sum(alg) if fused else alg[i]
         pl = ph[i] / frames
         kernels[n] = {"ms_per_launch": pl, "share": ph[i] / sum(ph), "alg_bytes_per_launch": bl,
                       "gbs": bl / (pl / 1e3) / 1e9}
         if i == 0:  # what the kernel moves: 37 reals + 2 flag bytes read, 25 reals written
             kernels[n]["moved_bytes_per_launch"] = nb * (62 * real + 2)
             kernels[n]["moved_gbs"] = nb * (62 * real + 2) / (pl / 1e3) / 1e9
+    traffic = RESOLVE_TRAFFIC.get(head) if default_size and dom == 2 and not fused else None
     info = batches[head].info()
     for b in batches.values():
         b.close()
@@ -393,8 +405,8 @@ def run_ours(args):
         "clocks": r32["clocks"],
         "roofline": {"kernel": phase_names[dom], "bound": "hbm", "achieved": achieved, "peak": peak,
                      "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
-                     "traffic": RESOLVE_TRAFFIC["bytes"] if default_size and dom == 2 else None,
-                     "traffic_source": dict(RESOLVE_TRAFFIC, bytes=None) if default_size and dom == 2 else None,
+                     "traffic": traffic["bytes"] if traffic else None,
+                     "traffic_source": dict(traffic, bytes=None) if traffic else None,
                      "note": "the resolver is sequential per world and latency / float64-pipe bound; its HBM "
                              "fraction is reported as asked, iterations per second below"},
         "resolver_iterations_per_s": (cnt["pos_iterations"] + cnt["vel_iterations"]) / (args.steps * ph[2] / 1e3),

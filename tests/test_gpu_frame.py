@@ -47,6 +47,9 @@ def test_fused_frame_sleep_offsets_and_timed(form, cuda_lib):
     sleepy.can_sleep[:] = 1
     for scene in (sleepy, scenes.offsets(num_worlds=8, bodies=24, seed=9)):
         gpu, ref = _fused(scene, form), OracleBatch(scene, form=form)
+        if scene is sleepy:  # bodies settle and fall asleep from about frame 300
+            gpu.step(360, DT)
+            ref.step(360, DT)
         gpu.prepare_rollout(120, DT)
         tot, ph = gpu.step_timed(120, DT)
         ref.step(120, DT)
@@ -54,7 +57,7 @@ def test_fused_frame_sleep_offsets_and_timed(form, cuda_lib):
         assert_bodies_equal(g, ref.bodies(), STATE + ("motion", "is_awake"))
         assert ph[0] == 0.0 and ph[1] == 0.0 and ph[2] > 0.0
         if scene is sleepy:
-            assert (g["is_awake"] == 0).sum() > 20  # bodies went to sleep
+            assert (g["is_awake"] == 0).sum() > 100  # bodies went to sleep
 
 
 def test_fused_frame_launches_and_fallbacks(cuda_lib):
