@@ -70,7 +70,8 @@ def tune(batch, frames=30, dt=1.0 / 60.0, lanes=DEFAULT_LANES, tiles=DEFAULT_TIL
     batch.set_tuning(resolver_lanes=best[0], resolver_contacts=best[1])
     # one launch per frame, where the batch allows it (one world per warp, no
     # world above the slot, the plain resolver): the batch ignores it otherwise
-    if fused and best[0] == 32 and not (np.asarray(batch.counts) > BIG_WORLD).any():
+    if (fused and best[0] == 32 and not getattr(batch, "warm_start", False)
+            and not (np.asarray(batch.counts) > BIG_WORLD).any()):
         best_f, f_ms = None, None
         for f in (-1, 1):
             batch.set_tuning(fused_frame=f)

@@ -43,6 +43,7 @@ class WorldBatch:
         self.num_worlds = int(self.counts.shape[0])
         self.num_bodies = int(self.counts.sum())
         self.form = form
+        self.warm_start = False  # set by learned.set_warm_start
         self.desc = {"plane": [float(x) for x in plane], "contact_capacity": int(contact_capacity),
                      "iteration_multiplier": int(iteration_multiplier), "max_iterations": int(max_iterations)}
         d = _lib.BatchDesc()

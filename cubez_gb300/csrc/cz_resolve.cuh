@@ -774,30 +774,39 @@ __device__ int warm_start_apply(const RCtx<R, W>& x, int n, int C, int gl, bool 
   return moved;
 }
 
+// Which resolved body each body of contact k is: e[b] = d when contact body
+// b is resolved body d (d1 < 0: there is none), else -1.  A contact body is
+// at most one of the two, so a contact takes at most two changes: body 0's
+// first, then body 1's, which is the order of the reference's (b, d) loops
+// (contact.go:254-280, 412-440).  The updates below run one code block per
+// contact body, with d taken from e, instead of one per (b, d) pair: a warp
+// runs a block whenever any of its lanes needs it.
+__device__ __forceinline__ int2 touching(int bb, int d0, int d1) {
+  const int kb0 = body0_of(bb), kb1 = body1_of(bb);
+  int2 e;
+  e.x = kb0 == d0 ? 0 : (d1 >= 0 && kb0 == d1 ? 1 : -1);
+  e.y = kb1 < 0 ? -1 : (kb1 == d0 ? 0 : (d1 >= 0 && kb1 == d1 ? 1 : -1));
+  return e;
+}
+
 // adjustPositions' update of contact k after resolving a contact between
 // bodies d0, d1 (d1 < 0: none) whose linear / angular changes are in x.bc
 // (contact.go:254-280); a contact touching neither is left alone.
 template <class R, class W>
 __device__ __forceinline__ void penetration_update(const RCtx<R, W>& x, int k, int d0, int d1) {
-  const int bb = x.cb[k];
-  const int kb[2] = {body0_of(bb), body1_of(bb)};
-  const bool m0 = kb[0] == d0 || (d1 >= 0 && kb[0] == d1);
-  const bool m1 = kb[1] >= 0 && (kb[1] == d0 || kb[1] == d1);
-  if (!m0 && !m1) return;
+  const int2 e = touching(x.cb[k], d0, d1);
+  if (e.x < 0 && e.y < 0) return;
   const v3<R> nk = x.Cv(W_NX, k);
   R pen = x.Cf(W_PEN, k);
 #pragma unroll
   for (int b = 0; b < 2; ++b) {
-    if (kb[b] < 0) continue;
-    const v3<R> r = b == 0 ? x.Cv(W_R0X, k) : x.Cv(W_R1X, k);
-#pragma unroll
-    for (int d = 0; d < 2; ++d) {
-      if (kb[b] == (d == 0 ? d0 : d1)) {
-        v3<R> dp = cross(V<R>(x.bc[6 + 3 * d], x.bc[7 + 3 * d], x.bc[8 + 3 * d]), r);
-        add(dp, V<R>(x.bc[3 * d], x.bc[3 * d + 1], x.bc[3 * d + 2]));
-        const R sign = b == 0 ? (R)-1 : (R)1;
-        pen += dot(dp, nk) * sign;
-      }
+    const int d = b == 0 ? e.x : e.y;
+    if (d >= 0) {
+      const v3<R> r = b == 0 ? x.Cv(W_R0X, k) : x.Cv(W_R1X, k);
+      v3<R> dp = cross(d == 0 ? V<R>(x.bc[6], x.bc[7], x.bc[8]) : V<R>(x.bc[9], x.bc[10], x.bc[11]), r);
+      add(dp, d == 0 ? V<R>(x.bc[0], x.bc[1], x.bc[2]) : V<R>(x.bc[3], x.bc[4], x.bc[5]));
+      const R sign = b == 0 ? (R)-1 : (R)1;
+      pen += dot(dp, nk) * sign;
     }
   }
   x.Cf(W_PEN, k) = pen;
@@ -806,27 +815,21 @@ __device__ __forceinline__ void penetration_update(const RCtx<R, W>& x, int k, i
 // adjustVelocities' update of contact k (contact.go:412-440), as above.
 template <class R, class W>
 __device__ __forceinline__ void velocity_update(const RCtx<R, W>& x, int k, int d0, int d1) {
-  const int bb = x.cb[k];
-  const int kb[2] = {body0_of(bb), body1_of(bb)};
-  const bool m0 = kb[0] == d0 || (d1 >= 0 && kb[0] == d1);
-  const bool m1 = kb[1] >= 0 && (kb[1] == d0 || kb[1] == d1);
-  if (!m0 && !m1) return;
+  const int2 e = touching(x.cb[k], d0, d1);
+  if (e.x < 0 && e.y < 0) return;
   const m3<R> Ck = x.basis(k);
   v3<R> cv = x.Cv(W_CVX, k);
 #pragma unroll
   for (int b = 0; b < 2; ++b) {
-    if (kb[b] < 0) continue;
-    const v3<R> r = b == 0 ? x.Cv(W_R0X, k) : x.Cv(W_R1X, k);
-#pragma unroll
-    for (int d = 0; d < 2; ++d) {
-      if (kb[b] == (d == 0 ? d0 : d1)) {
-        v3<R> dv = cross(V<R>(x.bc[6 + 3 * d], x.bc[7 + 3 * d], x.bc[8 + 3 * d]), r);
-        add(dv, V<R>(x.bc[3 * d], x.bc[3 * d + 1], x.bc[3 * d + 2]));
-        const R sign = b == 1 ? (R)-1 : (R)1;
-        v3<R> t = mulv_t(Ck, dv);
-        mul_with(t, sign);
-        add(cv, t);
-      }
+    const int d = b == 0 ? e.x : e.y;
+    if (d >= 0) {
+      const v3<R> r = b == 0 ? x.Cv(W_R0X, k) : x.Cv(W_R1X, k);
+      v3<R> dv = cross(d == 0 ? V<R>(x.bc[6], x.bc[7], x.bc[8]) : V<R>(x.bc[9], x.bc[10], x.bc[11]), r);
+      add(dv, d == 0 ? V<R>(x.bc[0], x.bc[1], x.bc[2]) : V<R>(x.bc[3], x.bc[4], x.bc[5]));
+      const R sign = b == 1 ? (R)-1 : (R)1;
+      v3<R> t = mulv_t(Ck, dv);
+      mul_with(t, sign);
+      add(cv, t);
     }
   }
   x.setCv(W_CVX, k, cv);

@@ -72,6 +72,7 @@ def set_warm_start(batch, blob):
         b = np.ascontiguousarray(blob, np.float32)
         assert b.shape == (BLOB,)
         check(L.cz_set_warm_start(batch.h, _ptr(b)))
+    batch.warm_start = blob is not None
 
 
 class Trainer:

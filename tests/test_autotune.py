@@ -66,3 +66,7 @@ def test_fused_frame_tried_with_one_world_per_warp():
     b = FakeBatch([32, 80])
     cfg, trials = autotune.tune(b, frames=2, lanes=(32,))
     assert not any("fused_frame" in t for t in trials)  # a world above the slot
+    b = FakeBatch([32] * 8)
+    b.warm_start = True
+    cfg, trials = autotune.tune(b, frames=2, lanes=(32,))
+    assert not any("fused_frame" in t for t in trials)  # the learned resolver
