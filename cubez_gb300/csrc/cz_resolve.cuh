@@ -9,9 +9,11 @@
 // runs for all groups at once, so each instruction of that chain serves
 // 32 / G worlds: on GB300 a float64 warp instruction costs the same pipe time
 // whatever its active mask, so packing worlds into a warp divides the float64
-// cost of the plain form and of the precision form's islands by 32 / G.  The
-// friction solve's matrices do not change during adjustVelocities and are
-// computed once per contact, off the chain (friction_prepare).
+// cost of the plain form and of the precision form's islands by 32 / G; with
+// 16 or 32 lanes per world the precision form's position island is spread
+// over 14 lanes of the group instead (apply_position_change).  The friction
+// solve's matrices do not change during adjustVelocities and are computed
+// once per contact, off the chain (friction_prepare).
 //
 // Groups of a warp advance in lockstep rounds; a group whose world is done
 // idles until the warp's last world finishes its phase.  Worlds are queued in
@@ -263,8 +265,20 @@ __device__ void derive_asleep(const RCtx<R, W>& x, const BatchView<R>& v, int bs
 // order (body 0, then body 1).  Each body's operations are the one-lane
 // formula's, so results are identical.  Lane i leaves body i's linear and
 // angular change in x.bc[3i..3i+2] and x.bc[6+3i..8+3i].
+//
+// In the precision form with at least 16 lanes per world, the float64
+// island is spread over the group: lanes 2-7 add one position component each
+// (body (gl-2)/3), lanes 8-15 one quaternion component each (body (gl-8)/4)
+// and square it; the quaternion's first lane sums the squares in the
+// reference's order and decides the renormalisation, which every component
+// lane applies.  A float64 warp instruction costs the pipe the same whatever
+// its active lanes, so this takes one float64 add for all fourteen
+// components (seven per body on one lane before) and one multiply for the
+// squares, and each lane converts one value.  The operations on every value
+// are the one-lane formula's.
 template <class R, class W, int G>
 __device__ void apply_position_change(const RCtx<R, W>& x, const BatchView<R>& v, int bstart, int k, bool on, int gl) {
+  constexpr bool kSpread = sizeof(R) != sizeof(W) && G >= 16;
   const bool mine = on && gl < 2;
   const R z = (R)0;
   int b = -1;
@@ -287,50 +301,138 @@ __device__ void apply_position_change(const RCtx<R, W>& x, const BatchView<R>& v
   const R angO = __shfl_sync(0xffffffffu, angI, gl ^ 1, G);
   const R linO = __shfl_sync(0xffffffffu, linI, gl ^ 1, G);
   const int bO = __shfl_sync(0xffffffffu, b, gl ^ 1, G);
-  if (!mine) return;
-  const int b0 = gl == 0 ? b : bO, b1 = gl == 0 ? bO : b;
-  R total = z;
-  if (b0 >= 0) total += (gl == 0 ? linI : linO) + (gl == 0 ? angI : angO);
-  if (b1 >= 0) total += (gl == 0 ? linO : linI) + (gl == 0 ? angO : angI);
+  if (!kSpread && !mine) return;
   v3<R> lin = V<R>(z, z, z), ang = V<R>(z, z, z);
-  if (b >= 0) {
-    const R sign = gl != 0 ? (R)-1 : (R)1;
-    R am = sign * penetration * (angI / total);
-    R lm = sign * penetration * (linI / total);
-    v3<R> proj = rp;
-    add_scaled(proj, n, -dot(rp, n));
-    const R maxm = (R)0.2 * mag(proj);
-    if (am < -maxm) {
-      R tm = am + lm;
-      am = -maxm;
-      lm = tm - am;
-    } else if (am > maxm) {
-      R tm = am + lm;
-      am = maxm;
-      lm = tm - am;
+  if (mine) {
+    const int b0 = gl == 0 ? b : bO, b1 = gl == 0 ? bO : b;
+    R total = z;
+    if (b0 >= 0) total += (gl == 0 ? linI : linO) + (gl == 0 ? angI : angO);
+    if (b1 >= 0) total += (gl == 0 ? linO : linI) + (gl == 0 ? angO : angI);
+    if (b >= 0) {
+      const R sign = gl != 0 ? (R)-1 : (R)1;
+      R am = sign * penetration * (angI / total);
+      R lm = sign * penetration * (linI / total);
+      v3<R> proj = rp;
+      add_scaled(proj, n, -dot(rp, n));
+      const R maxm = (R)0.2 * mag(proj);
+      if (am < -maxm) {
+        R tm = am + lm;
+        am = -maxm;
+        lm = tm - am;
+      } else if (am > maxm) {
+        R tm = am + lm;
+        am = maxm;
+        lm = tm - am;
+      }
+      if (am != (R)0) {
+        ang = mulv(x.iit(b), cross(rp, n));
+        mul_with(ang, am / angI);
+      }
+      lin = n;
+      mul_with(lin, lm);
+      if constexpr (!kSpread) {
+        // Position.AddScaled(normal, linearMove): product in R, accumulated in W
+        x.P(0, b) += cvt_fast<W>(n.x * lm);
+        x.P(1, b) += cvt_fast<W>(n.y * lm);
+        x.P(2, b) += cvt_fast<W>(n.z * lm);
+        q4<W> q{x.P(3, b), x.P(4, b), x.P(5, b), x.P(6, b)};
+        add_scaled_vector_island<R, W>(q, ang);
+        qnormalize_island<R, W>(q);
+        x.P(3, b) = q.w; x.P(4, b) = q.x; x.P(5, b) = q.y; x.P(6, b) = q.z;
+        if (!x.aw[b]) {
+          // CalculateDerivedData reads the stored (R-rounded) orientation
+          x.P(3, b) = (W)(R)q.w; x.P(4, b) = (W)(R)q.x; x.P(5, b) = (W)(R)q.y; x.P(6, b) = (W)(R)q.z;
+          derive_asleep(x, v, bstart, b);
+        }
+      }
     }
-    if (am != (R)0) {
-      ang = mulv(x.iit(b), cross(rp, n));
-      mul_with(ang, am / angI);
+    x.bc[3 * gl] = lin.x; x.bc[3 * gl + 1] = lin.y; x.bc[3 * gl + 2] = lin.z;
+    x.bc[6 + 3 * gl] = ang.x; x.bc[7 + 3 * gl] = ang.y; x.bc[8 + 3 * gl] = ang.z;
+  }
+  if constexpr (kSpread) {
+    const bool plane = gl >= 2 && gl < 8, qlane = gl >= 8 && gl < 16;
+    const int pc = (gl - 2) % 3, qc = (gl - 8) & 3;
+    const int src = plane ? (gl - 2) / 3 : (qlane ? (gl - 8) >> 2 : 0);  // the body's lane
+    const int bs = __shfl_sync(0xffffffffu, mine ? b : -1, src, G);
+    const bool act = (plane || qlane) && bs >= 0;
+    // the quaternion, narrowed by its component lanes for the increment
+    // (add_scaled_vector_island's first step)
+    W acc = (W)0;
+    R qr = z;
+    if (act && qlane) {
+      acc = x.P(3 + qc, bs);
+      qr = cvt_fast<R>(acc);
     }
-    lin = n;
-    mul_with(lin, lm);
-    // Position.AddScaled(normal, linearMove): product in R, accumulated in W
-    x.P(0, b) += cvt_fast<W>(n.x * lm);
-    x.P(1, b) += cvt_fast<W>(n.y * lm);
-    x.P(2, b) += cvt_fast<W>(n.z * lm);
-    q4<W> q{x.P(3, b), x.P(4, b), x.P(5, b), x.P(6, b)};
-    add_scaled_vector_island<R, W>(q, ang);
-    qnormalize_island<R, W>(q);
-    x.P(3, b) = q.w; x.P(4, b) = q.x; x.P(5, b) = q.y; x.P(6, b) = q.z;
-    if (!x.aw[b]) {
+    const int qsrc = 8 + 4 * (gl & 1);
+    const R r0 = __shfl_sync(0xffffffffu, qr, qsrc, G), r1 = __shfl_sync(0xffffffffu, qr, qsrc + 1, G);
+    const R r2 = __shfl_sync(0xffffffffu, qr, qsrc + 2, G), r3 = __shfl_sync(0xffffffffu, qr, qsrc + 3, G);
+    R h0 = z, h1 = z, h2 = z, h3 = z;
+    if (mine && b >= 0) {
+      const q4<R> qq{r0, r1, r2, r3};
+      q4<R> t{(R)0, ang.x * (R)1, ang.y * (R)1, ang.z * (R)1};
+      t = qmul(t, qq);
+      h0 = t.w * (R)0.5; h1 = t.x * (R)0.5; h2 = t.y * (R)0.5; h3 = t.z * (R)0.5;
+    }
+    const R H0 = __shfl_sync(0xffffffffu, h0, src, G), H1 = __shfl_sync(0xffffffffu, h1, src, G);
+    const R H2 = __shfl_sync(0xffffffffu, h2, src, G), H3 = __shfl_sync(0xffffffffu, h3, src, G);
+    const R L0 = __shfl_sync(0xffffffffu, lin.x, src, G), L1 = __shfl_sync(0xffffffffu, lin.y, src, G);
+    const R L2 = __shfl_sync(0xffffffffu, lin.z, src, G);
+    // one float64 add: lanes 2-7 Position.AddScaled(normal, linearMove),
+    // lanes 8-15 the quaternion increment
+    if (act) {
+      R val;
+      if (plane) {
+        acc = x.P(pc, bs);
+        val = pc == 0 ? L0 : (pc == 1 ? L1 : L2);
+      } else {
+        val = qc == 0 ? H0 : (qc == 1 ? H1 : (qc == 2 ? H2 : H3));
+      }
+      acc += cvt_fast<W>(val);
+      if (plane) x.P(pc, bs) = acc;
+    }
+    // qnormalize_island: the squares on the component lanes, the sum in
+    // order and the decision on the quaternion's first lane
+    const W sq = act && qlane ? acc * acc : (W)0;
+    const W s1 = __shfl_sync(0xffffffffu, sq, gl + 1, G), s2 = __shfl_sync(0xffffffffu, sq, gl + 2, G);
+    const W s3 = __shfl_sync(0xffffffffu, sq, gl + 3, G);
+    int mode = 0;  // 0: leave, 1: scale by inv, 2: the identity (a zero quaternion)
+    W inv = (W)0;
+    if (act && qlane && qc == 0) {
+      const W s = sq + s1 + s2 + s3;
+      const W e = s - (W)1;
+      const W ae = fabs(e);
+      if (ae < (W)4e-7) {
+      } else if (ae < (W)0x1p-11) {
+        inv = (W)1 + e * ((W)-0.5 + e * ((W)0.375 + e * ((W)-0.3125 + e * (W)0.2734375)));
+        mode = 1;
+      } else {  // Normalize, quaternion.go:77-99, on the same sum
+        W len = sqrt_<W>(s);
+        if (real_equal<W>((W)1, len)) {
+        } else if (len == (W)0) {
+          mode = 2;
+        } else {
+          if (len == Lim<W>::inf()) len = Lim<W>::max_value();
+          inv = (W)1 / len;
+          mode = 1;
+        }
+      }
+    }
+    const int lead = qlane ? gl - qc : 0;
+    mode = __shfl_sync(0xffffffffu, mode, lead, G);
+    inv = __shfl_sync(0xffffffffu, inv, lead, G);
+    if (act && qlane) {
+      if (mode == 1) acc *= inv;
+      else if (mode == 2) acc = qc == 0 ? (W)1 : (W)0;
+      x.P(3 + qc, bs) = acc;
+    }
+    __syncwarp();
+    if (mine && b >= 0 && !x.aw[b]) {
       // CalculateDerivedData reads the stored (R-rounded) orientation
-      x.P(3, b) = (W)(R)q.w; x.P(4, b) = (W)(R)q.x; x.P(5, b) = (W)(R)q.y; x.P(6, b) = (W)(R)q.z;
+#pragma unroll
+      for (int c = 3; c < 7; ++c) x.P(c, b) = (W)(R)x.P(c, b);
       derive_asleep(x, v, bstart, b);
     }
   }
-  x.bc[3 * gl] = lin.x; x.bc[3 * gl + 1] = lin.y; x.bc[3 * gl + 2] = lin.z;
-  x.bc[6 + 3 * gl] = ang.x; x.bc[7 + 3 * gl] = ang.y; x.bc[8 + 3 * gl] = ang.z;
 }
 
 template <class R> __device__ __forceinline__ m3<R> skew(const v3<R>& v) {  // contact.go:612-616
@@ -1042,9 +1144,11 @@ __device__ void frame_front(const BatchView<R>& v, int w, int n, int bstart, int
 // fused frame): each world's integrate and narrowphase first
 // (frame_front), so one launch runs a whole frame (one world per warp, plain
 // resolver).
+// Registers: one world per warp in float32 is bounded to 18 CTAs per SM (96
+// registers, a few spilled), the count its shared-memory slot allows.
 template <class R, class W, int G, bool LEARN, bool FRAME = false>
 __global__ void __launch_bounds__(32, FRAME ? (sizeof(R) == 4 ? 18 : 8)
-                                            : (LEARN ? (G == 32 && sizeof(R) == 4 ? 18 : 16) : 0))
+                                            : (G == 32 && sizeof(R) == 4 ? 18 : (LEARN ? 16 : 0)))
     k_resolve(BatchView<R> v, int nbs, int cs, R dt, R sleep_bias = (R)0) {
   static_assert(!FRAME || (G == 32 && !LEARN), "the fused frame runs one world per warp, plain");
   extern __shared__ __align__(128) unsigned char smem[];
