@@ -266,19 +266,20 @@ __device__ void derive_asleep(const RCtx<R, W>& x, const BatchView<R>& v, int bs
 // formula's, so results are identical.  Lane i leaves body i's linear and
 // angular change in x.bc[3i..3i+2] and x.bc[6+3i..8+3i].
 //
-// In the precision form with at least 16 lanes per world, the float64
-// island is spread over the group: lanes 2-7 add one position component each
-// (body (gl-2)/3), lanes 8-15 one quaternion component each (body (gl-8)/4)
-// and square it; the quaternion's first lane sums the squares in the
-// reference's order and decides the renormalisation, which every component
-// lane applies.  A float64 warp instruction costs the pipe the same whatever
-// its active lanes, so this takes one float64 add for all fourteen
-// components (seven per body on one lane before) and one multiply for the
-// squares, and each lane converts one value.  The operations on every value
-// are the one-lane formula's.
+// With at least 16 lanes per world, the updates of position and orientation
+// are spread over the group: lanes 2-7 add one position component each (body
+// (gl-2)/3), lanes 8-15 one quaternion component each (body (gl-8)/4) and
+// square it; the quaternion's first lane sums the squares in the reference's
+// order and decides the renormalisation (the precision form's island, or
+// Normalize in the float64 form), which every component lane applies.  A
+// float64 warp instruction costs the pipe the same whatever its active
+// lanes, so this takes one float64 add for all fourteen components (seven
+// per body on one lane before) and one multiply for the squares, and in the
+// precision form each lane converts one value.  The operations on every
+// value are the one-lane formula's.
 template <class R, class W, int G>
 __device__ void apply_position_change(const RCtx<R, W>& x, const BatchView<R>& v, int bstart, int k, bool on, int gl) {
-  constexpr bool kSpread = sizeof(R) != sizeof(W) && G >= 16;
+  constexpr bool kSpread = G >= 16;
   const bool mine = on && gl < 2;
   const R z = (R)0;
   int b = -1;
@@ -401,8 +402,8 @@ __device__ void apply_position_change(const RCtx<R, W>& x, const BatchView<R>& v
       const W s = sq + s1 + s2 + s3;
       const W e = s - (W)1;
       const W ae = fabs(e);
-      if (ae < (W)4e-7) {
-      } else if (ae < (W)0x1p-11) {
+      if (sizeof(R) != sizeof(W) && ae < (W)4e-7) {
+      } else if (sizeof(R) != sizeof(W) && ae < (W)0x1p-11) {
         inv = (W)1 + e * ((W)-0.5 + e * ((W)0.375 + e * ((W)-0.3125 + e * (W)0.2734375)));
         mode = 1;
       } else {  // Normalize, quaternion.go:77-99, on the same sum
