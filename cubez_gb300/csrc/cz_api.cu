@@ -89,8 +89,7 @@ struct cz_batch {
   int* cbodies = nullptr;
   void* work = nullptr;
   int* wbodies = nullptr;
-  void* kmat = nullptr;  // per contact: friction K (doubles) and response row (reals)
-  void* kdv = nullptr;
+  void* kmat = nullptr;  // per contact: friction K and response row, 16 reals
   int* d_order = nullptr;
   int* d_order_rs = nullptr;
   unsigned* d_queue = nullptr;
@@ -184,7 +183,6 @@ struct cz_batch {
     v.contact_bodies = cbodies;
     v.work = work;
     v.kmat = kmat;
-    v.kdv = kdv;
     v.work_bodies = wbodies;
     v.nc_total = nc_total;
     v.order = d_order;
@@ -289,7 +287,7 @@ void free_batch(cz_batch* b) {
       b->ws_world,  b->mlp_mem,     b->hv_features, b->hv_labels, b->hv_count,   b->snap_body,   b->snap_u8,
       b->body,      b->awake,       b->can_sleep, b->shape,       b->d_bstart,   b->d_bcount,    b->d_ccap,
       b->d_ccount,  b->d_cstart,    b->d_wstatus, b->d_piters,    b->d_viters,   b->contact,     b->cbodies,
-      b->work,      b->wbodies,     b->kmat,      b->kdv,         b->d_order,    b->d_order_rs,  b->d_queue,
+      b->work,      b->wbodies,     b->kmat,      b->d_order,    b->d_order_rs,  b->d_queue,
       b->d_status,  b->d_counters,  b->d_h2p,     b->d_stage,     b->d_stage_u8, b->d_stage_i32, b->d_cstage,
       b->d_cstage_b, b->d_pow};
   for (void* p : dev)
@@ -571,7 +569,7 @@ int cz_batch_create(const cz_batch_desc* d, cz_batch** out) {
        dmalloc((void**)&b->d_order, sizeof(int) * W) && dmalloc((void**)&b->d_order_rs, sizeof(int) * W);
   ok = ok && dmalloc(&b->contact, R * cz::C_NROWS * C) && dmalloc((void**)&b->cbodies, sizeof(int) * C);
   ok = ok && dmalloc(&b->work, R * cz::W_NROWS * C) && dmalloc((void**)&b->wbodies, sizeof(int) * C);
-  ok = ok && dmalloc(&b->kmat, sizeof(double) * 9 * C) && dmalloc(&b->kdv, R * 3 * C);
+  ok = ok && dmalloc(&b->kmat, R * cz::K_ROW * C);
   ok = ok && dmalloc((void**)&b->d_queue, 4 * sizeof(unsigned)) && dmalloc((void**)&b->d_status, sizeof(uint32_t)) &&
        dmalloc((void**)&b->d_counters, 8 * sizeof(unsigned long long));
   ok = ok && dmalloc((void**)&b->d_h2p, sizeof(int) * std::max<long long>(nb, 1));

@@ -31,8 +31,7 @@ static BatchView<R> view_of(const HostView& h) {
   v.contact = static_cast<R*>(h.contact);
   v.contact_bodies = h.contact_bodies;
   v.work = static_cast<R*>(h.work);
-  v.kmat = h.kmat;
-  v.kdv = static_cast<R*>(h.kdv);
+  v.kmat = static_cast<R*>(h.kmat);
   v.work_bodies = h.work_bodies;
   v.nc_total = h.nc_total;
   v.order = h.order;

@@ -34,8 +34,7 @@ struct HostView {
   int* contact_bodies;
   void* work;
   int* work_bodies;
-  void* kmat;  // [9][nc_total] doubles
-  void* kdv;   // [3][nc_total] reals
+  void* kmat;  // [nc_total][16] reals
   long long nc_total;
   const int* order;
   const int* order_rs;

@@ -62,6 +62,10 @@ enum WorkRow : int {
   W_J0, W_J1, W_J2,  // contact-frame impulse: predicted (warm start) or applied in total (harvest)
   W_NROWS
 };
+// reals per contact of the friction solve's matrices (K: 9, the response's
+// first row: 3, padding: 4), contact-major, so the resolved contact's are one
+// aligned 64- (float32) or 128-byte (float64) block
+constexpr int K_ROW = 16;
 // whether the form stores the basis tangent row
 template <class R> __host__ __device__ constexpr bool stores_tangent() { return true; }
 // rows the resolver keeps per contact in its shared-memory tile
@@ -110,8 +114,8 @@ template <class R> struct BatchView {
   R* contact;           // [C_NROWS][nc_total]
   int* contact_bodies;  // [nc_total]
   R* work;              // [W_NROWS][nc_total]
-  void* kmat;           // [9][nc_total] reals: K of each contact's friction solve (inverted in the island type)
-  R* kdv;               // [3][nc_total]: the friction response's first row
+  R* kmat;              // [nc_total][16] reals per contact: K of its friction solve (9, inverted in the
+                        // island type), the friction response's first row (3), padding (4)
   int* work_bodies;     // [nc_total]
   long long nc_total;
   const int* order;     // narrowphase queue: worlds in decreasing body count

@@ -57,9 +57,8 @@ template <class R, class W> struct RCtx {
   long long wst;
   R* jw;          // impulse rows J0..J2 (row stride jst)
   long long jst;
-  R* kw;          // per contact: K of the friction solve (inverted in W, kept in R), 9 rows (row stride kst)
-  R* kr;          // per contact: the response matrix's first row, 3 rows
-  long long kst;
+  R* kw;          // per contact, K_ROW reals: K of the friction solve (inverted in W, kept in R), 9,
+                  // then the response matrix's first row, 3
   const R* gmat;  // friction / restitution rows of the contact list (null: 0.9 / 0.1)
   long long gst;
   R dt;
@@ -67,8 +66,8 @@ template <class R, class W> struct RCtx {
   __device__ __forceinline__ R& Bf(int r, int i) const { return br[r * nbs + i]; }
   __device__ __forceinline__ R& Cf(int f, int k) const { return cw[(long long)f * cst + k]; }
   __device__ __forceinline__ R& J(int c, int k) const { return jw[(long long)c * jst + k]; }
-  __device__ __forceinline__ R& K(int q, int k) const { return kw[(long long)q * kst + k]; }
-  __device__ __forceinline__ R& KD(int q, int k) const { return kr[(long long)q * kst + k]; }
+  __device__ __forceinline__ R& K(int q, int k) const { return kw[(long long)k * K_ROW + q]; }
+  __device__ __forceinline__ R& KD(int q, int k) const { return kw[(long long)k * K_ROW + 9 + q]; }
   __device__ __forceinline__ int& WI(int r, int i) const { return wi[(long long)r * wst + i]; }
   __device__ __forceinline__ R& Save(int r, int i) const { return save[(long long)r * wst + i]; }
   __device__ __forceinline__ R& Delta(int r, int i) const { return delta[(long long)r * wst + i]; }
@@ -498,10 +497,30 @@ template <class R, class W> __device__ __forceinline__ void friction_prepare(con
 // calculateFrictionImpulse, contact.go:533-606, from the matrices of
 // friction_prepare: the solve K * (desired delta velocity, -vy, -vz) in R,
 // then the dynamic-friction correction.
-template <class R, class W> __device__ v3<R> friction_impulse(const RCtx<R, W>& x, int k) {
-  m3<R> K;
+// A contact's K (the first 9 reals of its K_ROW block) by 16-byte loads, and
+// the response's first row (reals 9-11), which only the dynamic-friction
+// branch reads.
+__device__ __forceinline__ void load_k(const float* p, float (&o)[9]) {
+  const float4* q = reinterpret_cast<const float4*>(p);
+  const float4 a = q[0], b = q[1];
+  o[0] = a.x; o[1] = a.y; o[2] = a.z; o[3] = a.w;
+  o[4] = b.x; o[5] = b.y; o[6] = b.z; o[7] = b.w;
+  o[8] = p[8];
+}
+__device__ __forceinline__ void load_k(const double* p, double (&o)[9]) {
+  const double2* q = reinterpret_cast<const double2*>(p);
 #pragma unroll
-  for (int q = 0; q < 9; ++q) K.m[q] = x.K(q, k);
+  for (int i = 0; i < 4; ++i) {
+    const double2 t = q[i];
+    o[2 * i] = t.x; o[2 * i + 1] = t.y;
+  }
+  o[8] = p[8];
+}
+
+template <class R, class W> __device__ v3<R> friction_impulse(const RCtx<R, W>& x, int k) {
+  const R* row = x.kw + (long long)k * K_ROW;
+  m3<R> K;
+  load_k(row, K.m);
   const R ddv = x.Cf(W_DDV, k);
   const v3<R> kill = V<R>(ddv, -x.Cf(W_CVY, k), -x.Cf(W_CVZ, k));
   v3<R> ic = mulv(K, kill);
@@ -510,7 +529,7 @@ template <class R, class W> __device__ v3<R> friction_impulse(const RCtx<R, W>& 
   if (planar > ic.x * fr) {
     ic.y /= planar;
     ic.z /= planar;
-    ic.x = x.KD(0, k) + x.KD(1, k) * fr * ic.y + x.KD(2, k) * fr * ic.z;
+    ic.x = row[9] + row[10] * fr * ic.y + row[11] * fr * ic.z;
     ic.x = ddv / ic.x;
     ic.y *= fr * ic.x;
     ic.z *= fr * ic.x;
@@ -661,9 +680,7 @@ __device__ __forceinline__ void bind_contacts(Slot<R, W>& s, const BatchView<R>&
   }
   x.gmat = v.uniform_material ? nullptr : v.contact + (long long)C_FRIC * v.nc_total + cst;
   x.gst = (long long)(C_REST - C_FRIC) * v.nc_total;
-  x.kw = reinterpret_cast<R*>(v.kmat) + cst;
-  x.kr = v.kdv + cst;
-  x.kst = v.nc_total;
+  x.kw = v.kmat + cst * K_ROW;
 }
 
 // the learned paths' global scratch of the world whose bodies start at bstart
@@ -1493,8 +1510,6 @@ __global__ void __launch_bounds__(32 * kWfWarps) k_warm_features(BatchView<R> v,
   x.bc = nullptr;
   x.save = x.delta = nullptr;
   x.kw = nullptr;
-  x.kr = nullptr;
-  x.kst = 0;
   const bool harvest = v.mode == 1;
   for (;;) {
     unsigned q = 0;

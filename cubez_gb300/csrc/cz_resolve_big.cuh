@@ -125,9 +125,7 @@ __global__ void __launch_bounds__(32) k_resolve_big(BatchView<R> v, R dt) {
   x.save = x.delta = x.jw = nullptr;
   x.wi = nullptr;
   x.wst = x.jst = 0;
-  x.kw = reinterpret_cast<R*>(v.kmat) + cst;
-  x.kr = v.kdv + cst;
-  x.kst = v.nc_total;
+  x.kw = v.kmat + cst * K_ROW;
   const bool active = has && C > 0 && dt > (R)0;  // ResolveContacts guards, contact.go:210-212
   if (has && !active && gl == 0) {
     v.pos_iters[w] = 0;

@@ -48,8 +48,7 @@ constexpr size_t kOffCBodies = align256(kOffContact + sizeof(double) * cz::C_NRO
 constexpr size_t kOffWork = align256(kOffCBodies + sizeof(int) * kStaticMaxContacts);
 constexpr size_t kOffWBodies = align256(kOffWork + sizeof(double) * cz::W_NROWS * kStaticMaxContacts);
 constexpr size_t kOffKmat = align256(kOffWBodies + sizeof(int) * kStaticMaxContacts);
-constexpr size_t kOffKdv = align256(kOffKmat + sizeof(double) * 9 * kStaticMaxContacts);
-constexpr size_t kOffMeta = align256(kOffKdv + sizeof(double) * 3 * kStaticMaxContacts);
+constexpr size_t kOffMeta = align256(kOffKmat + sizeof(double) * cz::K_ROW * kStaticMaxContacts);
 constexpr size_t kScratchBytes = align256(kOffMeta + 256);
 
 static __device__ __align__(256) unsigned char g_static_scratch[kScratchBytes];
@@ -222,7 +221,6 @@ cz::HostView static_view(unsigned char* scratch, int n) {
   v.work = scratch + kOffWork;
   v.work_bodies = reinterpret_cast<int*>(scratch + kOffWBodies);
   v.kmat = scratch + kOffKmat;
-  v.kdv = scratch + kOffKdv;
   v.nc_total = kStaticMaxContacts;
   v.order = &m->order;
   v.order_rs = &m->order_rs;
