@@ -42,7 +42,7 @@ template <class R> __device__ __forceinline__ v3<R> contact_tangent(const v3<R>&
 
 template <class R, class W> struct RCtx {
   W* bw;          // [7][nbs]: position xyz, orientation wxyz (island type)
-  R* br;          // [20][nbs]: vel 0-2, rot 3-5, lfa 6-8, iitWorld 9-17, invMass 18, motion 19
+  R* br;          // [20][nbs]: vel 0-2, rot 3-5, lfa * dt 6-8, iitWorld 9-17, invMass 18, motion 19
   uint8_t* aw;    // [nbs] awake
   int nbs;
   R* cw;          // working rows of this world's contacts
@@ -160,16 +160,10 @@ template <class R, class W> __device__ __forceinline__ R desired_dv(const RCtx<R
   const int b0 = body0_of(bb), b1 = body1_of(bb);
   const v3<R> n = x.Cv(W_NX, k);
   R vfa = (R)0;
-  if (x.aw[b0]) {
-    v3<R> t = x.Bv(6, b0);
-    mul_with(t, x.dt);
-    vfa += dot(t, n);
-  }
-  if (b1 >= 0 && x.aw[b1]) {
-    v3<R> t = x.Bv(6, b1);
-    mul_with(t, x.dt);
-    vfa -= dot(t, n);
-  }
+  // rows 6-8 hold LastFrameAcceleration * duration, formed when the body is
+  // loaded (the reference's product, once instead of at every use)
+  if (x.aw[b0]) vfa += dot(x.Bv(6, b0), n);
+  if (b1 >= 0 && x.aw[b1]) vfa -= dot(x.Bv(6, b1), n);
   R rest = x.restitution(k);
   const R cvx = x.Cf(W_CVX, k);
   if (fabs_<R>(cvx) < (R)0.25) rest = (R)0;
@@ -182,8 +176,7 @@ __device__ __forceinline__ v3<R> local_velocity(const RCtx<R, W>& x, int body, c
   v3<R> vel = cross(x.Bv(3, body), rp);
   add(vel, x.Bv(0, body));
   v3<R> cv = mulv_t(C, vel);
-  v3<R> acc = x.Bv(6, body);
-  mul_with(acc, x.dt);
+  v3<R> acc = x.Bv(6, body);  // LastFrameAcceleration * duration
   acc = mulv_t(C, acc);
   acc.x = (R)0;
   add(cv, acc);
@@ -604,7 +597,7 @@ __device__ __forceinline__ void load_bodies(const RCtx<R, W>& x, const BatchView
     for (int r = 0; r < 3; ++r) {
       x.Bf(r, i) = v.body[(B_VX + r) * S + g];
       x.Bf(3 + r, i) = v.body[(B_RX + r) * S + g];
-      x.Bf(6 + r, i) = v.body[(B_LX + r) * S + g];
+      x.Bf(6 + r, i) = v.body[(B_LX + r) * S + g] * x.dt;
     }
 #pragma unroll
     for (int r = 0; r < 9; ++r) x.Bf(9 + r, i) = v.body[(B_IW0 + r) * S + g];

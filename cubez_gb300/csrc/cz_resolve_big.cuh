@@ -147,7 +147,7 @@ __global__ void __launch_bounds__(32) k_resolve_big(BatchView<R> v, R dt) {
     for (int r = 0; r < 3; ++r) {
       x.Bf(r, i) = v.body[(B_VX + r) * S + g];
       x.Bf(3 + r, i) = v.body[(B_RX + r) * S + g];
-      x.Bf(6 + r, i) = v.body[(B_LX + r) * S + g];
+      x.Bf(6 + r, i) = v.body[(B_LX + r) * S + g] * x.dt;  // LastFrameAcceleration * duration
     }
 #pragma unroll
     for (int r = 0; r < 9; ++r) x.Bf(9 + r, i) = v.body[(B_IW0 + r) * S + g];
