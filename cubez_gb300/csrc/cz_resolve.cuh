@@ -2,7 +2,8 @@
 //
 // One warp holds 32 / G worlds; the G lanes of a group own one world.  Within
 // a group the contacts are lane-strided: the argmax is a G-lane butterfly
-// whose tie-break is the reference's first-maximum rule, and the
+// (warp reductions for G = 32) whose tie-break is the reference's
+// first-maximum rule, and the
 // per-iteration update of every contact touching the two resolved bodies is
 // lane-parallel.  The sequential part of an iteration (applyPositionChange
 // on lanes 0 and 1, one body each; applyVelocityChange on the group leader)
@@ -138,8 +139,8 @@ __device__ __forceinline__ void warp_first_max(unsigned long long& key, int& idx
 
 // Largest key over the G lanes of a group, smallest index among equal keys
 // (the first maximum of the reference's scan, contact.go:238-245, 394-402).
-template <int G, bool REDUX = true, class K> __device__ __forceinline__ void group_first_max(K& key, int& idx) {
-  if constexpr (G == 32 && REDUX) {
+template <int G, class K> __device__ __forceinline__ void group_first_max(K& key, int& idx) {
+  if constexpr (G == 32) {
     warp_first_max(key, idx);
     return;
   }
@@ -969,7 +970,7 @@ __device__ int velocity_loop(const RCtx<R, W>& x, const BatchView<R>& v, int w, 
       }
     }
   while (__any_sync(FULL, run)) {
-    group_first_max<G, !LEARN>(best, bidx);
+    group_first_max<G>(best, bidx);
     if (best == 0) run = false;
     if (run && gl == 0) {
       match_awake(x, x.cb[bidx]);
@@ -1235,7 +1236,7 @@ __global__ void __launch_bounds__(32, FRAME ? (sizeof(R) == 4 ? 18 : 8)
         }
       }
     while (__any_sync(FULL, run)) {
-      group_first_max<G, !LEARN>(best, bidx);
+      group_first_max<G>(best, bidx);
       if (best == 0) run = false;
       if (run && gl == 0) match_awake(x, x.cb[bidx]);
       __syncwarp();
