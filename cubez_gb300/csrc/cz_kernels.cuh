@@ -434,18 +434,14 @@ template <class R>
 __device__ int pair_full(const NPTile<R>& tl, int i, int j, const BatchView<R>& v, int bstart, NPContact<R>& c,
                          uint32_t& err) {
   const int si = tl.shape[i], sj = tl.shape[j];
-  if (sj == 0) {
-    if (si == 0)
-      return sphere_sphere(V<R>(tl.T[9 * tl.nbs + i], tl.T[10 * tl.nbs + i], tl.T[11 * tl.nbs + i]), tl.radius(i), i,
-                           V<R>(tl.T[9 * tl.nbs + j], tl.T[10 * tl.nbs + j], tl.T[11 * tl.nbs + j]), tl.radius(j), j,
-                           c);
-    return cube_sphere(tl.xform(i), tl.half(i), i, tl.xform(j), tl.radius(j), j,
-                       v.body + (long long)B_VX * v.nb_pad + bstart + j, v.nb_pad, c);
-  }
-  if (si == 0)
-    return cube_sphere(tl.xform(j), tl.half(j), j, tl.xform(i), tl.radius(i), i,
-                       v.body + (long long)B_VX * v.nb_pad + bstart + i, v.nb_pad, c);
-  return cube_cube(tl.xform(i), tl.half(i), i, tl.xform(j), tl.half(j), j, c, err);
+  if (si == 0 && sj == 0)
+    return sphere_sphere(V<R>(tl.T[9 * tl.nbs + i], tl.T[10 * tl.nbs + i], tl.T[11 * tl.nbs + i]), tl.radius(i), i,
+                         V<R>(tl.T[9 * tl.nbs + j], tl.T[10 * tl.nbs + j], tl.T[11 * tl.nbs + j]), tl.radius(j), j, c);
+  if (si != 0 && sj != 0) return cube_cube(tl.xform(i), tl.half(i), i, tl.xform(j), tl.half(j), j, c, err);
+  // a cube and a sphere, in either order: one call site
+  const int bx = si != 0 ? i : j, sp = si != 0 ? j : i;
+  return cube_sphere(tl.xform(bx), tl.half(bx), bx, tl.xform(sp), tl.radius(sp), sp,
+                     v.body + (long long)B_VX * v.nb_pad + bstart + sp, v.nb_pad, c);
 }
 
 template <class R>
@@ -506,6 +502,9 @@ __device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned pari
 // CTA (256), and at least one body's units (the grid path lists a body's
 // units together).
 constexpr int kSurvivors = 512;
+// np_flush's scratch for a CTA of bd threads: the chunk's order by kind of
+// test, its counts, and per-kind counts of each warp (6 kinds x 8 warps)
+__host__ __device__ constexpr int np_sort_ints(int bd) { return 2 * bd + 64; }
 __host__ __device__ inline int np_surv_cap(int nbs) { return nbs + 1 > kSurvivors ? ((nbs + 32) & ~31) : kSurvivors; }
 
 template <class R> __host__ __device__ inline size_t np_smem_bytes(int nbs) {
@@ -515,6 +514,7 @@ template <class R> __host__ __device__ inline size_t np_smem_bytes(int nbs) {
   b += (size_t)5 * nbs * sizeof(float);           // cull data
   b += 2 * 33 * sizeof(int);                      // scan scratch (double-buffered) + world id + wait outcome
   b += (size_t)np_surv_cap(nbs) * sizeof(int);    // units past the culls, awaiting their full tests
+  b += (size_t)np_sort_ints(256) * sizeof(int);   // np_flush's sort of a chunk by kind of test
   return b;
 }
 
@@ -628,17 +628,53 @@ __device__ __forceinline__ void np_emit(const NPTile<R>& tl, const BatchView<R>&
 }
 
 // The full tests of the listed units (unit u = i * n + k: k = 0 the
-// half-space, else the pair with j = k - 1, skipping i), in list order and in
-// chunks of the CTA's size, emitting their contacts at out onwards.
+// half-space, else the pair with j = k - 1, skipping i), in chunks of the
+// CTA's size, emitting their contacts in list order at out onwards.  Within a
+// chunk the units are taken in order of their kind of test (half-space with
+// a sphere, with a cube; sphere-sphere, sphere-cube, cube-cube), stably, so
+// the lanes of a warp mostly run one test's code; the counts are then
+// scanned in list order, so every contact lands where the list order puts
+// it (the reference's contact order).  sortw: np_sort_ints(blockDim.x) ints.
 template <class R>
 __device__ void np_flush(const NPTile<R>& tl, const BatchView<R>& v, int bstart, int n, long long cs, int cap,
-                         const int* surv, int nsurv, int* scan, int& parity, int& out, uint32_t& err) {
-  for (int sb = 0; sb < nsurv; sb += blockDim.x) {
-    const int si = sb + threadIdx.x;
+                         const int* surv, int nsurv, int* scan, int& parity, int& out, uint32_t& err, int* sortw) {
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5, bd = blockDim.x, nwarps = (bd + 31) >> 5;
+  int* perm = sortw;
+  int* cntb = sortw + bd;
+  int* wcnt = sortw + 2 * bd;  // [kind * 8 + warp]
+  for (int sb = 0; sb < nsurv; sb += bd) {
+    const int m = nsurv - sb < bd ? nsurv - sb : bd;
+    int key = 5;  // no unit
+    if (tid < m) {
+      const int uu = surv[sb + tid];
+      const int i = uu / n, k = uu - i * n;
+      if (k == 0) {
+        key = tl.shape[i] != 0 ? 1 : 0;
+      } else {
+        int j = k - 1;
+        if (j >= i) ++j;
+        key = 2 + (tl.shape[i] != 0 ? 1 : 0) + (tl.shape[j] != 0 ? 1 : 0);
+      }
+    }
+    int rank = 0;
+#pragma unroll
+    for (int q = 0; q < 6; ++q) {
+      const unsigned bal = __ballot_sync(FULL, key == q);
+      if (key == q) rank = __popc(bal & ((1u << lane) - 1u));
+      if (lane == 0) wcnt[q * 8 + wid] = __popc(bal);
+    }
+    __syncthreads();
+    int dst = rank;
+    for (int q = 0; q < key; ++q)
+      for (int w2 = 0; w2 < nwarps; ++w2) dst += wcnt[q * 8 + w2];
+    for (int w2 = 0; w2 < wid; ++w2) dst += wcnt[key * 8 + w2];
+    perm[dst] = tid;
+    __syncthreads();
+    const int src = perm[tid];  // this thread tests the chunk's unit src
     int cnt = 0, i = 0, k = 0;
     NPContact<R> c;
-    if (si < nsurv) {
-      const int uu = surv[si];
+    if (src < m) {
+      const int uu = surv[sb + src];
       i = uu / n;
       k = uu - i * n;
       if (k == 0) {
@@ -649,11 +685,16 @@ __device__ void np_flush(const NPTile<R>& tl, const BatchView<R>& v, int bstart,
         cnt = pair_full<R>(tl, i, j, v, bstart, c, err);
       }
     }
+    cntb[src] = cnt;
+    __syncthreads();
     int excl, total;
-    np_chunk_scan(cnt, scan, parity, &excl, &total);
+    np_chunk_scan(cntb[tid], scan, parity, &excl, &total);  // list order
     parity ^= 1;
-    np_emit<R>(tl, v, cs, cap, out + excl, cnt, i, k == 0, c);
+    cntb[tid] = excl;
+    __syncthreads();
+    np_emit<R>(tl, v, cs, cap, out + cntb[src], cnt, i, k == 0, c);
     out += total;
+    __syncthreads();  // perm and cntb are reused by the next chunk
   }
 }
 
@@ -878,7 +919,7 @@ __device__ void np_world(const NPTile<R>& tl, const BatchView<R>& v, int w, int 
       }
       __syncthreads();
       nsurv = g.info[5];
-      np_flush(tl, v, bstart, n, cs, cap, surv, nsurv, scan, chunk_parity, out, err);
+      np_flush(tl, v, bstart, n, cs, cap, surv, nsurv, scan, chunk_parity, out, err, surv + scap);
       __syncthreads();
       ib += m;
     }
@@ -904,7 +945,7 @@ __device__ void np_world(const NPTile<R>& tl, const BatchView<R>& v, int w, int 
       nsurv += total;
       if (nsurv <= scap - (int)blockDim.x && base + (int)blockDim.x < U) continue;
       __syncthreads();
-      np_flush(tl, v, bstart, n, cs, cap, surv, nsurv, scan, chunk_parity, out, err);
+      np_flush(tl, v, bstart, n, cs, cap, surv, nsurv, scan, chunk_parity, out, err, surv + scap);
       nsurv = 0;
       __syncthreads();
     }

@@ -1111,7 +1111,7 @@ constexpr int kFrameSurvivors = 128;
 // and collider transforms, shapes, cull data, scan scratch, survivor list.
 template <class R> __host__ __device__ inline size_t frame_tile_bytes(int nbs) {
   size_t b = (size_t)(11 + 12) * nbs * sizeof(R) + (size_t)nbs * sizeof(int) + (size_t)5 * nbs * sizeof(float);
-  b += (66 + kFrameSurvivors) * sizeof(int);
+  b += (66 + kFrameSurvivors + np_sort_ints(32)) * sizeof(int);
   return (b + 15) & ~(size_t)15;
 }
 // The fused frame's slot: the resolver's, large enough for the narrowphase
