@@ -498,10 +498,10 @@ __device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned pari
   return false;
 }
 
-// Units past the culls held for their full tests: at least twice the largest
-// CTA (256), and at least one body's units (the grid path lists a body's
-// units together).
-constexpr int kSurvivors = 512;
+// Units past the culls held for their full tests: room for a round of culls
+// (up to 1024 units) on top of a partly filled list, and at least one body's
+// units (the grid path lists a body's units together).
+constexpr int kSurvivors = 1280;
 // np_flush's scratch for a CTA of bd threads: the chunk's order by kind of
 // test, its counts, and per-kind counts of each warp (6 kinds x 8 warps)
 __host__ __device__ constexpr int np_sort_ints(int bd) { return 2 * bd + 64; }
@@ -924,26 +924,36 @@ __device__ void np_world(const NPTile<R>& tl, const BatchView<R>& v, int w, int 
       ib += m;
     }
   } else {
-    // All pairs: the culls run over every unit; the units they keep are
-    // listed in unit order and get their full tests in chunks of the CTA's
-    // size, so the lanes of a warp run the costly tests together.
-    // Counting, scanning and emitting in list order keeps the reference's
-    // contact order.
-    for (int base = 0; base < U; base += blockDim.x) {
-      const int u = base + tid;
-      bool keep = false;
-      if (u < U) {
-        const int i = u / n, k = u - i * n;
-        int j = k - 1;
-        if (j >= i) ++j;
-        keep = k == 0 ? !plane_culled(tl, i, v) : !pair_culled(tl, i, j);
+    // All pairs: the culls run over every unit, upt consecutive units per
+    // thread and one scan per round; the units they keep are listed in unit
+    // order and get their full tests in chunks of the CTA's size, so the
+    // lanes of a warp run the costly tests together.  Counting, scanning and
+    // emitting in list order keeps the reference's contact order.
+    const int bd = blockDim.x;
+    int upt = (scap - bd) / bd;
+    upt = upt < 1 ? 1 : (upt > 8 ? 8 : upt);
+    const int round = bd * upt;  // at most scap - bd: the list never overflows
+    for (int base = 0; base < U; base += round) {
+      const int u0 = base + tid * upt;
+      unsigned keep = 0;
+      if (u0 < U) {
+        int i = u0 / n, k = u0 - i * n;
+        for (int q = 0; q < upt && u0 + q < U; ++q) {
+          int j = k - 1;
+          if (j >= i) ++j;
+          if (k == 0 ? !plane_culled(tl, i, v) : !pair_culled(tl, i, j)) keep |= 1u << q;
+          if (++k == n) {
+            k = 0;
+            ++i;
+          }
+        }
       }
       int excl, total;
-      np_chunk_scan(keep ? 1 : 0, scan, chunk_parity, &excl, &total);
+      np_chunk_scan(__popc(keep), scan, chunk_parity, &excl, &total);
       chunk_parity ^= 1;
-      if (keep) surv[nsurv + excl] = u;
+      for (int o = nsurv + excl; keep; keep &= keep - 1) surv[o++] = u0 + __ffs(keep) - 1;
       nsurv += total;
-      if (nsurv <= scap - (int)blockDim.x && base + (int)blockDim.x < U) continue;
+      if (nsurv <= scap - round && base + round < U) continue;
       __syncthreads();
       np_flush(tl, v, bstart, n, cs, cap, surv, nsurv, scan, chunk_parity, out, err, surv + scap);
       nsurv = 0;
