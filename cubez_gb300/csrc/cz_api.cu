@@ -230,16 +230,21 @@ namespace {
 // independent worlds does not change any result.
 constexpr int kReorderBuckets = 2048;
 __global__ void __launch_bounds__(1024) k_reorder(const int* __restrict__ pos_it, const int* __restrict__ vel_it,
-                                                  int W, int* __restrict__ order) {
+                                                  int W, int* __restrict__ order,
+                                                  const uint8_t* __restrict__ plain_next = nullptr) {
   __shared__ int hist[kReorderBuckets];
   __shared__ int wsum[32];
   const int tid = threadIdx.x;
   for (int i = tid; i < kReorderBuckets; i += blockDim.x) hist[i] = 0;
   __syncthreads();
-  for (int w = tid; w < W; w += blockDim.x) {
-    const int key = min(pos_it[w] + vel_it[w], kReorderBuckets - 1);
-    atomicAdd(&hist[kReorderBuckets - 1 - key], 1);
-  }
+  // with the warm start on, the worlds it will serve (plain_next[w] == 0)
+  // go first: their solve is usually short, but one that falls back solves
+  // twice, and late in the queue that would be the frame's tail
+  auto key_of_world = [&](int w) {
+    if (plain_next && !plain_next[w]) return kReorderBuckets - 1;
+    return min(pos_it[w] + vel_it[w], kReorderBuckets - 1);
+  };
+  for (int w = tid; w < W; w += blockDim.x) atomicAdd(&hist[kReorderBuckets - 1 - key_of_world(w)], 1);
   __syncthreads();
   // exclusive scan of 2048 buckets, two per thread
   const int a = hist[2 * tid], c = hist[2 * tid + 1];
@@ -267,10 +272,7 @@ __global__ void __launch_bounds__(1024) k_reorder(const int* __restrict__ pos_it
   hist[2 * tid] = excl;
   hist[2 * tid + 1] = excl + a;
   __syncthreads();
-  for (int w = tid; w < W; w += blockDim.x) {
-    const int key = min(pos_it[w] + vel_it[w], kReorderBuckets - 1);
-    order[atomicAdd(&hist[kReorderBuckets - 1 - key], 1)] = w;
-  }
+  for (int w = tid; w < W; w += blockDim.x) order[atomicAdd(&hist[kReorderBuckets - 1 - key_of_world(w)], 1)] = w;
 }
 
 void free_batch(cz_batch* b) {
@@ -375,7 +377,8 @@ int launch_resolve_with(cz_batch* b, double dt, const cz::HostView& v, int cs, s
     CZ_CUDA(b->ops->resolve(v, b->rs_nbs, cs, b->rs_lanes, b->rs_grid, smem, dt, b->stream));
     g_launches++;
     if (b->nsmall > 32 / b->rs_lanes) {
-      k_reorder<<<1, 1024, 0, b->stream>>>(b->d_piters, b->d_viters, b->num_worlds, b->d_order_rs);
+      k_reorder<<<1, 1024, 0, b->stream>>>(b->d_piters, b->d_viters, b->num_worlds, b->d_order_rs,
+                                           v.mode == 2 ? v.ws_world : nullptr);
       CZ_CUDA(cudaGetLastError());
       g_launches++;
     }
