@@ -360,6 +360,7 @@ def run_ours(args):
     if rank != 0:
         return
     cpu = None if args.no_cpu_baseline else cpu_baseline(args, scene)
+    secondary = None if (args.no_secondary or ws > 1) else secondary_samples(local)
     def block(name):
         if name not in results:
             return None
@@ -413,8 +414,55 @@ def run_ours(args):
         "batch": info,
         "tuning": tuning,
         "cpu_baseline": cpu,
+        "secondary": secondary,
     }
     print(json.dumps(line))
+
+
+def _sample_rollout(scene, form, frames, local, units=None, warmup=1):
+    """`warmup` untimed rollouts and one timed rollout of `frames` frames
+    (default tuning): body-steps/s, and pair-tests/s of the narrowphase when
+    `units` (tests per frame) is given."""
+    import torch
+    from cubez_gb300.batch import WorldBatch
+    b = WorldBatch.from_scene(scene, form=form, device=local)
+    b.prepare_rollout(frames, DT)  # the graph capture, untimed
+    b.snapshot()
+    for _ in range(warmup):
+        b.step_timed(frames, DT)
+        b.restore()
+    _flush_l2()
+    clocks = Clocks(local)
+    with clocks:
+        torch.cuda.synchronize()
+        tot, ph = b.step_timed(frames, DT)
+    b.close()
+    r = {"ms_per_step": tot, "phase_ms": [float(x) for x in ph], "clocks": clocks.summary(),
+         "body_steps_per_s": scene.num_bodies * frames / (tot / 1e3)}
+    if units is not None:
+        r["pair_tests_per_s"] = units * frames / (ph[1] / 1e3)
+    return r
+
+
+def secondary_samples(local):
+    """One rollout of each secondary configuration at its full size, so that
+    the default run records them too (default tuning, one timed rollout; the
+    tuned runs with more steps: --workload piles / batched): 64 cube piles of
+    1024 bodies over 60 frames in both forms, and the batched float64 worlds
+    (4096 x U{8..64}) over 600 frames."""
+    from cubez_gb300 import scenes
+    from cubez_gb300.batch import FORM_FP32, FORM_FP64
+    piles = scenes.piles(num_worlds=64, seed=5)
+    n = int(piles.counts[0])
+    units = piles.num_worlds * (n * (n - 1) + n)
+    out = {"piles": {"workload": "64 worlds x %d cubes, 60 frames, default tuning, one timed rollout per form" % n,
+                     "fp32": _sample_rollout(piles, FORM_FP32, 60, local, units),
+                     "fp64": _sample_rollout(piles, FORM_FP64, 60, local, units, warmup=0)}}
+    mixed = scenes.mixed(num_worlds=4096, seed=2)
+    out["batched_fp64"] = {"workload": "4096 worlds x U{8..64} (%d bodies), 600 frames, float64, default tuning, "
+                                       "one timed rollout" % mixed.num_bodies,
+                           "fp64": _sample_rollout(mixed, FORM_FP64, 600, local, warmup=0)}
+    return out
 
 
 def cpu_baseline(args, scene):
@@ -726,6 +774,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-accuracy", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-secondary", action="store_true", help="skip the short piles / batched samples")
     args = ap.parse_args()
     import sys as _sys
     args.warmup_given = any(a.startswith("--warmup") for a in _sys.argv[1:])

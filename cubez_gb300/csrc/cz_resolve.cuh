@@ -155,20 +155,23 @@ template <int G, class K> __device__ __forceinline__ void group_first_max(K& key
   }
 }
 
-// calculateDesiredDeltaVelocity, contact.go:87-112
-template <class R, class W> __device__ __forceinline__ R desired_dv(const RCtx<R, W>& x, int k) {
-  const int bb = x.cb[k];
-  const int b0 = body0_of(bb), b1 = body1_of(bb);
-  const v3<R> n = x.Cv(W_NX, k);
+// calculateDesiredDeltaVelocity, contact.go:87-112, of contact k between
+// bodies b0, b1 with normal n and contact velocity x component cvx (the
+// callers pass what they hold in registers).
+template <class R, class W>
+__device__ __forceinline__ R desired_dv_of(const RCtx<R, W>& x, int k, int b0, int b1, const v3<R>& n, R cvx) {
   R vfa = (R)0;
   // rows 6-8 hold LastFrameAcceleration * duration, formed when the body is
   // loaded (the reference's product, once instead of at every use)
   if (x.aw[b0]) vfa += dot(x.Bv(6, b0), n);
   if (b1 >= 0 && x.aw[b1]) vfa -= dot(x.Bv(6, b1), n);
   R rest = x.restitution(k);
-  const R cvx = x.Cf(W_CVX, k);
   if (fabs_<R>(cvx) < (R)0.25) rest = (R)0;
   return -cvx - rest * (cvx - vfa);
+}
+template <class R, class W> __device__ __forceinline__ R desired_dv(const RCtx<R, W>& x, int k) {
+  const int bb = x.cb[k];
+  return desired_dv_of(x, k, body0_of(bb), body1_of(bb), x.Cv(W_NX, k), x.Cf(W_CVX, k));
 }
 
 // calculateLocalVelocity, contact.go:158-182
@@ -929,7 +932,8 @@ __device__ __forceinline__ void penetration_update(const RCtx<R, W>& x, int k, i
 // adjustVelocities' update of contact k (contact.go:412-440), as above.
 template <class R, class W>
 __device__ __forceinline__ void velocity_update(const RCtx<R, W>& x, int k, int d0, int d1) {
-  const int2 e = touching(x.cb[k], d0, d1);
+  const int bb = x.cb[k];
+  const int2 e = touching(bb, d0, d1);
   if (e.x < 0 && e.y < 0) return;
   const m3<R> Ck = x.basis(k);
   v3<R> cv = x.Cv(W_CVX, k);
@@ -947,7 +951,7 @@ __device__ __forceinline__ void velocity_update(const RCtx<R, W>& x, int k, int 
     }
   }
   x.setCv(W_CVX, k, cv);
-  x.Cf(W_DDV, k) = desired_dv(x, k);
+  x.Cf(W_DDV, k) = desired_dv_of(x, k, body0_of(bb), body1_of(bb), V<R>(Ck.m[0], Ck.m[1], Ck.m[2]), cv.x);
 }
 
 // adjustVelocities, contact.go:388-445, for the groups with run set; returns
