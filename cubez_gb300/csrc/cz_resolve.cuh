@@ -616,9 +616,9 @@ __device__ __forceinline__ void load_bodies(const RCtx<R, W>& x, const BatchView
 // broadcast scratch, packed bodies, awake flags.  The learned paths keep
 // their per-body scratch and the impulse rows in global memory, so they use
 // the same slot (and reach the same occupancy) as the plain resolver.
-// The float64 form with one world per warp gathers the contacts touching the
-// two resolved bodies before updating them (see position_loop_w); room for
-// one gather.
+// The float64 form (8 or more lanes per world) gathers the contacts touching
+// the two resolved bodies before updating them (see position_loop_g); room
+// for one gather.
 constexpr int kTouchList = 64;
 template <class R> __host__ __device__ constexpr bool gathers_updates() { return sizeof(R) == 8; }
 
@@ -1004,100 +1004,119 @@ __device__ int velocity_loop(const RCtx<R, W>& x, const BatchView<R>& v, int w, 
 }
 
 // ---------------------------------------------------------------- gathered updates
-// The float64 form with one world per warp updates, after a resolved
-// contact, only the contacts touching its two bodies: gathered in contact
-// order (a ballot per 32 contacts) and updated one per lane, instead of every
-// lane walking all its contacts, where a matching contact's float64 update
-// ran once per loop position with a match anywhere in the warp, at the cost
-// of a whole warp instruction on the float64 pipe for each.  The reference's
-// loop visits every contact but changes only these, and each update touches
-// only its own contact (contact.go:254-280, 412-440), so the result is the
-// same bit for bit.  (In float32 the gather did not pay: the same number of
-// instructions, and more registers.)
+// The float64 form updates, after a resolved contact, only the contacts
+// touching its two bodies: gathered in contact order (a ballot per G
+// contacts of each world) and updated one per lane of the world's group,
+// instead of every lane walking all its contacts, where a matching contact's
+// float64 update ran once per loop position with a match anywhere in the
+// warp, at the cost of a whole warp instruction on the float64 pipe for
+// each.  The reference's loop visits every contact but changes only these,
+// and each update touches only its own contact (contact.go:254-280,
+// 412-440), so the result is the same bit for bit.  The next argmax is then
+// a separate scan of the world's keys.  With G < 32 the worlds of a warp do
+// this side by side (lockstep, as the other loops).  (In float32 the gather
+// did not pay: the same number of instructions, and more registers.)
 
-// Applies upd(k) to every contact k touching body d0 or d1.
-template <class R, class W, class F>
-__device__ __forceinline__ void update_touching(const RCtx<R, W>& x, int C, int lane, int d0, int d1, int* ml,
+// Applies upd(k) to every contact k of the group's world touching body d0 or
+// d1 (nothing where `on` is false).  Every lane of the warp calls it.
+template <int G, class R, class W, class F>
+__device__ __forceinline__ void update_touching(const RCtx<R, W>& x, int C, int gl, int d0, int d1, int* ml, bool on,
                                                 F&& upd) {
+  const int lane = threadIdx.x & 31;
+  const unsigned gmask = G == 32 ? FULL : (((1u << G) - 1u) << (lane - gl));
+  const int Cg = on ? C : 0;
+  int Cmax = Cg;  // the warp's trip count: the largest of its worlds'
+#pragma unroll
+  for (int off = G; off < 32; off <<= 1) Cmax = max(Cmax, __shfl_xor_sync(FULL, Cmax, off));
   int m = 0;
-  for (int base = 0; base < C; base += 32) {
-    const int k = base + lane;
+  for (int base = 0; base < Cmax; base += G) {
+    const int k = base + gl;
     bool hit = false;
-    if (k < C) {
+    if (k < Cg) {
       const int bb = x.cb[k];
       const int kb0 = body0_of(bb), kb1 = body1_of(bb);
       hit = kb0 == d0 || (d1 >= 0 && kb0 == d1) || (kb1 >= 0 && (kb1 == d0 || kb1 == d1));
     }
-    const unsigned bal = __ballot_sync(FULL, hit);
+    const unsigned bal = __ballot_sync(FULL, hit) & gmask;
     if (hit) ml[m + __popc(bal & ((1u << lane) - 1u))] = k;
     m += __popc(bal);
-    if (m > kTouchList - 32 || base + 32 >= C) {
+    if (__any_sync(FULL, m > kTouchList - G) || base + G >= Cmax) {
       __syncwarp();
-      for (int j = lane; j < m; j += 32) upd(ml[j]);
+      for (int j = gl; j < m; j += G) upd(ml[j]);
       __syncwarp();
       m = 0;
     }
   }
 }
 
-// The warp's first maximum of a row's keys (W_PEN or W_DDV) over the world's
-// contacts.
-template <class R, class W>
-__device__ __forceinline__ void warp_row_first_max(const RCtx<R, W>& x, int row, int C, int lane,
-                                                   decltype(key_of((R)0, (R)0))& best, int& bidx) {
+// The group's first maximum of a row's keys (W_PEN or W_DDV) over its
+// world's contacts (key 0 where `on` is false).
+template <int G, class R, class W>
+__device__ __forceinline__ void group_row_first_max(const RCtx<R, W>& x, int row, int C, int gl, bool on,
+                                                    decltype(key_of((R)0, (R)0))& best, int& bidx) {
   best = key_of((R)0, (R)0);
   bidx = 0x7fffffff;
-  for (int k = lane; k < C; k += 32) {
+  for (int k = gl; on && k < C; k += G) {
     const auto key = key_of(x.Cf(row, k), (R)0.01);
     if (key > best) {
       best = key;
       bidx = k;
     }
   }
-  warp_first_max(best, bidx);
+  group_first_max<G>(best, bidx);
 }
 
-// adjustPositions (contact.go:231-283), one world per warp, gathered updates.
-template <class R, class W>
-__device__ int position_loop_w(const RCtx<R, W>& x, const BatchView<R>& v, int bstart, int C, int lane, int max_it,
+// adjustPositions (contact.go:231-283) with gathered updates, G lanes per
+// world; returns the iterations used.
+template <class R, class W, int G>
+__device__ int position_loop_g(const RCtx<R, W>& x, const BatchView<R>& v, int bstart, int C, int gl, int max_it,
                                bool run, int* ml) {
   int used = 0;
-  while (run) {
+  while (__any_sync(FULL, run)) {
     decltype(key_of((R)0, (R)0)) best;
     int bidx;
-    warp_row_first_max(x, W_PEN, C, lane, best, bidx);
-    if (best == 0) break;
-    if (lane == 0) match_awake(x, x.cb[bidx]);
+    group_row_first_max<G>(x, W_PEN, C, gl, run, best, bidx);
+    if (best == 0) run = false;
+    if (run && gl == 0) match_awake(x, x.cb[bidx]);
     __syncwarp();
-    apply_position_change<R, W, 32>(x, v, bstart, bidx, true, lane);
+    apply_position_change<R, W, G>(x, v, bstart, bidx, run, gl);
     __syncwarp();
-    const int rb = x.cb[bidx];
-    const int d0 = body0_of(rb), d1 = body1_of(rb);
-    update_touching(x, C, lane, d0, d1, ml, [&](int k) { penetration_update(x, k, d0, d1); });
-    if (++used >= max_it) break;
+    int d0 = -2, d1 = -2;
+    if (run) {
+      const int rb = x.cb[bidx];
+      d0 = body0_of(rb);
+      d1 = body1_of(rb);
+    }
+    update_touching<G>(x, C, gl, d0, d1, ml, run, [&](int k) { penetration_update(x, k, d0, d1); });
+    if (run && ++used >= max_it) run = false;
   }
   return used;
 }
 
-// adjustVelocities (contact.go:388-445), one world per warp, gathered updates.
-template <class R, class W, bool LEARN>
-__device__ int velocity_loop_w(const RCtx<R, W>& x, const BatchView<R>& v, int w, int C, int lane, int max_it,
+// adjustVelocities (contact.go:388-445) with gathered updates, G lanes per
+// world; returns the iterations used.
+template <class R, class W, int G, bool LEARN>
+__device__ int velocity_loop_g(const RCtx<R, W>& x, const BatchView<R>& v, int w, int C, int gl, int max_it,
                                bool run, int* ml) {
   int used = 0;
-  while (run) {
+  while (__any_sync(FULL, run)) {
     decltype(key_of((R)0, (R)0)) best;
     int bidx;
-    warp_row_first_max(x, W_DDV, C, lane, best, bidx);
-    if (best == 0) break;
-    if (lane == 0) {
+    group_row_first_max<G>(x, W_DDV, C, gl, run, best, bidx);
+    if (best == 0) run = false;
+    if (run && gl == 0) {
       match_awake(x, x.cb[bidx]);
       apply_velocity_change<R, W, LEARN>(x, v, w, bidx);
     }
     __syncwarp();
-    const int rb = x.cb[bidx];
-    const int d0 = body0_of(rb), d1 = body1_of(rb);
-    update_touching(x, C, lane, d0, d1, ml, [&](int k) { velocity_update(x, k, d0, d1); });
-    if (++used >= max_it) break;
+    int d0 = -2, d1 = -2;
+    if (run) {
+      const int rb = x.cb[bidx];
+      d0 = body0_of(rb);
+      d1 = body1_of(rb);
+    }
+    update_touching<G>(x, C, gl, d0, d1, ml, run, [&](int k) { velocity_update(x, k, d0, d1); });
+    if (run && ++used >= max_it) run = false;
   }
   return used;
 }
@@ -1221,11 +1240,11 @@ __global__ void __launch_bounds__(32, FRAME ? (sizeof(R) == 4 ? 18 : 8)
       for (int k = gl; k < C; k += G) prepare_contact(x, v, cst + k, k);
     __syncwarp();
     const int max_it = v.max_iterations >= 0 ? v.max_iterations : C * v.iter_mult;
-    constexpr bool kGather = G == 32 && gathers_updates<R>();
+    constexpr bool kGather = G >= 8 && gathers_updates<R>();
     // ---------------- adjustPositions, contact.go:231-283
     int used = 0;
     if constexpr (kGather) {
-      used = position_loop_w(x, v, bstart, C, lane, max_it, active && max_it > 0, sl.ml);
+      used = position_loop_g<R, W, G>(x, v, bstart, C, gl, max_it, active && max_it > 0, sl.ml);
     } else {
     bool run = active && max_it > 0;
     // as in velocity_loop: the update pass also finds the next argmax
@@ -1318,7 +1337,7 @@ __global__ void __launch_bounds__(32, FRAME ? (sizeof(R) == 4 ? 18 : 8)
     }
     // ---------------- adjustVelocities, contact.go:388-445
     if constexpr (kGather)
-      used = velocity_loop_w<R, W, LEARN>(x, v, w, C, lane, max_it, solve, sl.ml);
+      used = velocity_loop_g<R, W, G, LEARN>(x, v, w, C, gl, max_it, solve, sl.ml);
     else
       used = velocity_loop<R, W, G, LEARN>(x, v, w, C, gl, max_it, solve);
     int vel_used = used;
@@ -1358,7 +1377,7 @@ __global__ void __launch_bounds__(32, FRAME ? (sizeof(R) == 4 ? 18 : 8)
         __syncwarp();
         int used2;
         if constexpr (kGather)
-          used2 = velocity_loop_w<R, W, LEARN>(x, v, w, C, lane, max_it, fb, sl.ml);
+          used2 = velocity_loop_g<R, W, G, LEARN>(x, v, w, C, gl, max_it, fb, sl.ml);
         else
           used2 = velocity_loop<R, W, G, LEARN>(x, v, w, C, gl, max_it, fb);
         if (fb) vel_used += used2;
