@@ -582,6 +582,121 @@ __device__ void apply_velocity_change(const RCtx<R, W>& x, const BatchView<R>& v
 }
 
 
+// applyVelocityChange (contact.go:447-494) spread over lanes 0-5 of a group
+// with `on` (every lane of the warp calls it), for the float64 form, whose
+// chain runs on the float64 pipe: a float64 warp instruction costs the pipe
+// the same whatever its active lanes, so lane c (c = gl % 3) forms component
+// c of the friction solve's product and of the impulse, and lane 3i + c
+// forms component c of body i's velocity and rotation changes, where one
+// lane formed them all before.  Every component is the one-lane formula's
+// (mulv's row, cross's component, add_scaled), so the results are identical.
+// Lane 3i + c leaves body i's changes in x.bc[3i + c] and x.bc[6 + 3i + c].
+template <class R, class W, int G, bool LEARN>
+__device__ void apply_velocity_change_spread(const RCtx<R, W>& x, const BatchView<R>& v, int w, int k, bool on,
+                                             int gl) {
+  const int g0 = (threadIdx.x & 31) - gl;  // the group's first lane
+  const int c = gl % 3, i = gl / 3;
+  const int p = c == 2 ? 0 : c + 1, q = c == 0 ? 2 : c - 1;  // cross component c = a_p b_q - a_q b_p
+  const bool mine = on && gl < 6;
+  const R z = (R)0;
+  int b0 = 0, b1 = -1;
+  m3<R> C;
+  v3<R> ic = V<R>(z, z, z);
+  R icc = z;
+  bool frictionless = false;
+  if (on) {
+    const int bb = x.cb[k];
+    b0 = body0_of(bb);
+    b1 = body1_of(bb);
+    C = x.basis(k);
+    frictionless = x.friction(k) == (R)0;
+    if (frictionless) {
+      // calculateFrictionlessImpulse, contact.go:496-531 (rare: every lane)
+      v3<R> d = cross(x.Cv(W_R0X, k), x.Cv(W_NX, k));
+      d = mulv(x.iit(b0), d);
+      d = cross(d, x.Cv(W_R0X, k));
+      R dvel = dot(d, x.Cv(W_NX, k));
+      dvel += x.Bf(18, b0);
+      if (b1 < 0 && gl == 0) {
+        atomicOr(&v.world_status[w], ST_FRICTIONLESS_NIL);
+        atomicOr(v.status, ST_FRICTIONLESS_NIL);
+      }
+      ic = V<R>(x.Cf(W_DDV, k) / dvel, z, z);
+    } else {
+      // component c of K * (desired delta velocity, -vy, -vz) (mulv's row c)
+      const R* row = x.kw + (long long)k * K_ROW;
+      const R kx = x.Cf(W_DDV, k), ky = -x.Cf(W_CVY, k), kz = -x.Cf(W_CVZ, k);
+      icc = row[c] * kx + row[3 + c] * ky + row[6 + c] * kz;
+    }
+  }
+  {
+    const R i0 = __shfl_sync(FULL, icc, g0, 32), i1 = __shfl_sync(FULL, icc, g0 + 1, 32);
+    const R i2 = __shfl_sync(FULL, icc, g0 + 2, 32);
+    if (on && !frictionless) {
+      ic = V<R>(i0, i1, i2);
+      // calculateFrictionImpulse's dynamic friction, contact.go:586-604 (every lane)
+      const R* row = x.kw + (long long)k * K_ROW;
+      const R fr = x.friction(k);
+      const R ddv = x.Cf(W_DDV, k);
+      R planar = sqrt_<R>(ic.y * ic.y + ic.z * ic.z);
+      if (planar > ic.x * fr) {
+        ic.y /= planar;
+        ic.z /= planar;
+        ic.x = row[9] + row[10] * fr * ic.y + row[11] * fr * ic.z;
+        ic.x = ddv / ic.x;
+        ic.y *= fr * ic.x;
+        ic.z *= fr * ic.x;
+      }
+    }
+  }
+  if (LEARN && on && v.mode == 1 && gl == 0) {  // harvest: total impulse applied at this contact
+    x.J(0, k) += ic.x;
+    x.J(1, k) += ic.y;
+    x.J(2, k) += ic.z;
+  }
+  // component c of the impulse C * ic (mulv's row c)
+  R impc = z;
+  if (on) {
+    const R m0 = c == 0 ? C.m[0] : (c == 1 ? C.m[1] : C.m[2]);
+    const R m3 = c == 0 ? C.m[3] : (c == 1 ? C.m[4] : C.m[5]);
+    const R m6 = c == 0 ? C.m[6] : (c == 1 ? C.m[7] : C.m[8]);
+    impc = m0 * ic.x + m3 * ic.y + m6 * ic.z;
+  }
+  const R ix = __shfl_sync(FULL, impc, g0, 32), iy = __shfl_sync(FULL, impc, g0 + 1, 32);
+  const R iz = __shfl_sync(FULL, impc, g0 + 2, 32);
+  const v3<R> imp = V<R>(ix, iy, iz);
+  const int b = i == 0 ? b0 : b1;
+  const bool act = mine && b >= 0;
+  // component c of cross(r0, imp) (body 0) or cross(imp, r1) (body 1)
+  R crc = z;
+  v3<R> r = V<R>(z, z, z);
+  if (act) {
+    r = i == 0 ? x.Cv(W_R0X, k) : x.Cv(W_R1X, k);
+    const v3<R> a = i == 0 ? r : imp, bv = i == 0 ? imp : r;
+    const R ap = p == 0 ? a.x : (p == 1 ? a.y : a.z), aq = q == 0 ? a.x : (q == 1 ? a.y : a.z);
+    const R bp = p == 0 ? bv.x : (p == 1 ? bv.y : bv.z), bq = q == 0 ? bv.x : (q == 1 ? bv.y : bv.z);
+    crc = ap * bq - aq * bp;
+  }
+  const int t0 = g0 + 3 * (gl < 6 ? i : 0);
+  const R cx = __shfl_sync(FULL, crc, t0, 32), cy = __shfl_sync(FULL, crc, t0 + 1, 32);
+  const R cz = __shfl_sync(FULL, crc, t0 + 2, 32);
+  R vc = z, rc = z;
+  if (act) {
+    // rc = iitWorld * cross (mulv's row c); vc = 0 + imp * (+-inverse mass)
+    rc = x.Bf(9 + c, b) * cx + x.Bf(12 + c, b) * cy + x.Bf(15 + c, b) * cz;
+    const R im = i == 0 ? x.Bf(18, b) : -x.Bf(18, b);
+    const R impc_own = c == 0 ? imp.x : (c == 1 ? imp.y : imp.z);
+    vc += impc_own * im;
+    x.Bf(c, b) += vc;
+    x.Bf(3 + c, b) += rc;
+  }
+  if (mine) {
+    x.bc[3 * i + c] = vc;
+    x.bc[6 + 3 * i + c] = rc;
+  }
+}
+
+
 // A world's body rows from the batch rows into the working rows of x, by the
 // `step` lanes of a group (lane index `first`).
 template <class R, class W>
@@ -1104,7 +1219,11 @@ __device__ int velocity_loop_g(const RCtx<R, W>& x, const BatchView<R>& v, int w
     int bidx;
     group_row_first_max<G>(x, W_DDV, C, gl, run, best, bidx);
     if (best == 0) run = false;
-    if (run && gl == 0) {
+    if constexpr (sizeof(R) == 8) {
+      if (run && gl == 0) match_awake(x, x.cb[bidx]);
+      __syncwarp();
+      apply_velocity_change_spread<R, W, G, LEARN>(x, v, w, bidx, run, gl);
+    } else if (run && gl == 0) {
       match_awake(x, x.cb[bidx]);
       apply_velocity_change<R, W, LEARN>(x, v, w, bidx);
     }
