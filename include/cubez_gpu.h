@@ -195,9 +195,8 @@ int cz_batch_info(cz_batch* batch, int64_t* info /* [9] */);
  *   Scratch: a statically reserved device array of about 2.8 MB that every
  *   GPU loading the library holds until exit; hence the limits of at most 64
  *   bodies and 8192 contacts (CZ_ERR_BAD_ARG beyond).  The first call on a
- *   device looks up the array's device address (set-up); make that first call
- *   before any stream capture.  All calls share the array, so calls whose GPU
- *   work overlaps race on it: serialise them. */
+ *   device also looks up the array's device address.  All calls share the
+ *   array, so calls whose GPU work overlaps race on it: serialise them. */
 int cz_resolve_contacts_static(int32_t form, int32_t max_iterations, cz_contact* contacts, int32_t ncontacts,
                                double duration, const cz_bodies* bodies, int32_t nbodies, void* stream);
 
