@@ -437,7 +437,8 @@ int configure(cz_batch* b) {
   if (b->rs_ctas_per_sm > 0) rsb = std::min(rsb, b->rs_ctas_per_sm);
   b->np_grid = (int)std::min<long long>(b->num_worlds, (long long)npb * b->sm_count);
   const long long groups = (std::max(b->nsmall, 1) + 32 / b->rs_lanes - 1) / (32 / b->rs_lanes);
-  b->rs_grid = (int)std::min<long long>(groups, (long long)rsb * b->sm_count);
+  const int wpc = b->ops->rs_wpc(b->rs_lanes);
+  b->rs_grid = (int)std::min<long long>((groups + wpc - 1) / wpc, (long long)rsb * b->sm_count);
   b->np_grid = std::max(b->np_grid, 1);
   b->rs_grid = std::max(b->rs_grid, 1);
   b->wf_grid = (int)std::min<long long>(std::max(b->nsmall, 1),

@@ -187,9 +187,11 @@ __global__ void k_set_rows(BatchView<R> v, int row, int nrows, const double* __r
 }
 
 static size_t np_smem(int nbs) { return np_smem_bytes<R>(nbs); }
+// warps per resolver CTA for G lanes per world (rs_wpc)
+static int rs_wpc_of(int lanes) { return lanes == 32 ? rs_wpc<R, 32, false>() : 1; }
 static size_t rs_smem(int nbs, int cs, int lanes, int mode) {
   (void)mode;  // the learned paths keep their scratch in global memory and registers
-  return (size_t)(32 / lanes) * rs_slot_bytes<R, W>(nbs, cs);
+  return (size_t)rs_wpc_of(lanes) * (32 / lanes) * rs_slot_bytes<R, W>(nbs, cs);
 }
 
 // the resolver instantiation for G lanes per world, plain or with the
@@ -255,11 +257,11 @@ static cudaError_t resolve(const HostView& h, int nbs, int cs, int lanes, int gr
                            cudaStream_t s) {
   const BatchView<R> v = view_of(h);
   const bool learn = h.mode != 0;
-#define CZ_LAUNCH_RS(G)                                                         \
-  if (learn)                                                                   \
-    k_resolve<R, W, G, true><<<grid, 32, smem, s>>>(v, nbs, cs, (R)dt);        \
-  else                                                                         \
-    k_resolve<R, W, G, false><<<grid, 32, smem, s>>>(v, nbs, cs, (R)dt);
+#define CZ_LAUNCH_RS(G)                                                                              \
+  if (learn)                                                                                        \
+    k_resolve<R, W, G, true><<<grid, 32 * rs_wpc<R, G, false>(), smem, s>>>(v, nbs, cs, (R)dt);      \
+  else                                                                                              \
+    k_resolve<R, W, G, false><<<grid, 32 * rs_wpc<R, G, false>(), smem, s>>>(v, nbs, cs, (R)dt);
   switch (lanes) {
     case 4: CZ_LAUNCH_RS(4) break;
     case 8: CZ_LAUNCH_RS(8) break;
@@ -357,7 +359,7 @@ static cudaError_t occupancy(int* npb, int np_threads, size_t nps, int* rsb, siz
   if (e != cudaSuccess) return e;
   const void* f = resolve_fn_mode(lanes, mode);  // the instantiation that runs (registers differ)
   if (!f) return cudaErrorInvalidValue;
-  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(rsb, f, 32, rss);
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(rsb, f, 32 * rs_wpc_of(lanes), rss);
 }
 
 static cudaError_t contacts_out(const HostView& h, long long start, int count, double* sg, int* bodies,
@@ -385,6 +387,7 @@ static cudaError_t set_rows(const HostView& h, int row, int nrows, const double*
 const FormOps CZ_FORM_OBJ = {sizeof(CZ_R),
                              CZ_FORM_NS::np_smem,
                              CZ_FORM_NS::rs_smem,
+                             CZ_FORM_NS::rs_wpc_of,
                              CZ_FORM_NS::prepare,
                              CZ_FORM_NS::integrate,
                              CZ_FORM_NS::narrowphase,

@@ -80,7 +80,8 @@ enum StageBlock : int {
 struct FormOps {
   size_t real_size;
   size_t (*np_smem)(int nbs);
-  size_t (*rs_smem)(int nbs, int cs, int lanes, int mode);  // per CTA (one warp, 32 / lanes worlds)
+  size_t (*rs_smem)(int nbs, int cs, int lanes, int mode);  // per CTA (rs_wpc warps, 32 / lanes worlds each)
+  int (*rs_wpc)(int lanes);                                   // warps per resolver CTA
   cudaError_t (*prepare)(size_t np_smem, size_t rs_smem, int lanes);  // function attributes
   cudaError_t (*integrate)(const HostView& v, double dt, double sleep_bias, int threads, cudaStream_t s);
   cudaError_t (*narrowphase)(const HostView& v, int nbs, int threads, int grid, size_t smem, cudaStream_t s);

@@ -1298,20 +1298,28 @@ __device__ void frame_front(const BatchView<R>& v, int w, int n, int bstart, int
 // fused frame): each world's integrate and narrowphase first
 // (frame_front), so one launch runs a whole frame (one world per warp, plain
 // resolver).
-// Registers: one world per warp in float32 is bounded to 18 CTAs per SM (96
-// registers, a few spilled), the count its shared-memory slot allows.
+// Warps per CTA: one world per warp in float32 runs four independent warps
+// per CTA (each its own slot and its own worlds from the queue), so the SM's
+// per-CTA shared-memory reserve is paid once per four slots: 5 CTAs of 4
+// warps (20 warps) fit where 18 one-warp CTAs did.
+template <class R, int G, bool FRAME> __host__ __device__ constexpr int rs_wpc() {
+  return sizeof(R) == 4 && G == 32 && !FRAME ? 4 : 1;
+}
+// Registers: one world per warp in float32 is bounded to 20 warps per SM (96
+// registers, a few spilled), the count its shared-memory slots allow.
 template <class R, class W, int G, bool LEARN, bool FRAME = false>
-__global__ void __launch_bounds__(32, FRAME ? (sizeof(R) == 4 ? 18 : 8)
-                                            : (G == 32 && sizeof(R) == 4 ? 18 : (LEARN ? 16 : 0)))
+__global__ void __launch_bounds__(32 * rs_wpc<R, G, FRAME>(),
+                                  FRAME ? (sizeof(R) == 4 ? 18 : 8)
+                                        : (G == 32 && sizeof(R) == 4 ? 5 : (LEARN ? 16 : 0)))
     k_resolve(BatchView<R> v, int nbs, int cs, R dt, R sleep_bias = (R)0) {
   static_assert(!FRAME || (G == 32 && !LEARN), "the fused frame runs one world per warp, plain");
   extern __shared__ __align__(128) unsigned char smem[];
   constexpr int NG = 32 / G;
-  const int lane = threadIdx.x;
+  const int lane = threadIdx.x & 31;
   const int grp = lane / G, gl = lane % G;
   const int mode = LEARN ? v.mode : 0;
   const size_t slot_bytes = FRAME ? frame_slot_bytes<R, W>(nbs, cs) : rs_slot_bytes<R, W>(nbs, cs);
-  Slot<R, W> sl = make_slot<R, W>(smem + (size_t)grp * slot_bytes, nbs, cs, dt);
+  Slot<R, W> sl = make_slot<R, W>(smem + (size_t)((threadIdx.x >> 5) * NG + grp) * slot_bytes, nbs, cs, dt);
   RCtx<R, W>& x = sl.x;
   const long long S = v.nb_pad;
   for (;;) {

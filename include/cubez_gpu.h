@@ -263,7 +263,8 @@ int cz_mlp_predict(cz_mlp* mlp, const float* features, int64_t n, float* impulse
 typedef struct cz_tuning {
   int32_t narrowphase_threads; /* CTA size of the narrowphase */
   int32_t resolver_contacts;   /* contacts kept in shared memory per world */
-  int32_t resolver_ctas_per_sm;/* resident resolver warps per SM */
+  int32_t resolver_ctas_per_sm;/* resident resolver CTAs per SM (a CTA is 4 independent warps in the
+                                  float32 form with 32 lanes per world, else 1 warp) */
   int32_t integrate_threads;
   int32_t resolver_lanes;      /* lanes per world in the resolver: 4, 8, 16 or 32 */
   int32_t warm_start_budget_shift; /* learned warm start: a world is warm-started when its last
