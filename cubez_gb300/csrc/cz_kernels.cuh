@@ -975,9 +975,11 @@ __device__ void np_world(const NPTile<R>& tl, const BatchView<R>& v, int w, int 
 }
 
 // GRID = false compiles the all-pairs path alone (worlds too small for the
-// grid), so its registers and occupancy stay those of that path.
+// grid), so its registers and occupancy stay those of that path; in float32
+// it is bounded to 64 registers (8 CTAs of 128 threads per SM instead of 6;
+// a few registers spill), which hides more of its barrier waits.
 template <class R, bool GRID>
-__global__ void __launch_bounds__(256) k_narrowphase(BatchView<R> v, int nbs) {
+__global__ void __launch_bounds__(256, sizeof(R) == 4 && !GRID ? 4 : 0) k_narrowphase(BatchView<R> v, int nbs) {
   extern __shared__ __align__(128) unsigned char smem[];
   unsigned long long* bar = reinterpret_cast<unsigned long long*>(smem);
   NPTile<R> tl;
