@@ -85,7 +85,7 @@ __device__ __forceinline__ void integrate_body(const BatchView<R>& v, long long 
 }
 
 template <class R, class W>
-__global__ void __launch_bounds__(256) k_integrate(BatchView<R> v, R dt, R sleep_bias) {
+__global__ void __launch_bounds__(256, sizeof(R) == 4 ? 4 : 0) k_integrate(BatchView<R> v, R dt, R sleep_bias) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= v.nb_pad) return;
   integrate_body<R, W>(v, i, dt, sleep_bias);
