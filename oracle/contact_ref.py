@@ -404,9 +404,10 @@ def _apply_velocity_change(c, bodies):  # contact.go:447-494
     return vel, rot
 
 
-def resolve_contacts(max_iterations, contacts, bodies, dt):
+def resolve_contacts(max_iterations, contacts, bodies, dt, trace=None):
     """ResolveContacts (contact.go:208-222); returns the iterations used by
-    adjustPositions and adjustVelocities."""
+    adjustPositions and adjustVelocities.  `trace` (a list), when given,
+    receives ("p", index) / ("v", index) for every contact resolved."""
     if dt <= 0.0 or not contacts:
         return 0, 0
     for b in bodies:
@@ -423,6 +424,8 @@ def resolve_contacts(max_iterations, contacts, bodies, dt):
         if index == len(contacts):
             break
         ct = contacts[index]
+        if trace is not None:
+            trace.append(("p", index))
         _match_awake_state(ct, bodies)
         lin, ang = _apply_position_change(ct, bodies, best)
         for c in contacts:
@@ -445,6 +448,8 @@ def resolve_contacts(max_iterations, contacts, bodies, dt):
         if index == len(contacts):
             break
         ct = contacts[index]
+        if trace is not None:
+            trace.append(("v", index))
         _match_awake_state(ct, bodies)
         vel, rot = _apply_velocity_change(ct, bodies)
         for c in contacts:

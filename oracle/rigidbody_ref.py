@@ -100,11 +100,12 @@ def integrate(b, dt):  # rigidbody.go:213-259, no forces or torques accumulated
             b["motion"] = rt(10 * SLEEP_EPSILON)
 
 
-def step(bodies, plane, dt, iter_mult=4, units=None):
+def step(bodies, plane, dt, iter_mult=4, units=None, trace=None):
     """One frame of examples/cubedrop.go:69-75 (with the batch's iteration
     multiplier), or with `units` a caller's test list in place of the
     all-pairs order (examples/ballistic.go:47-104); returns (contacts,
-    adjustPositions and adjustVelocities iterations)."""
+    adjustPositions and adjustVelocities iterations).  `trace`: see
+    contact_ref.resolve_contacts."""
     for b in bodies:
         integrate(b, dt)
     if units is None:
@@ -112,5 +113,5 @@ def step(bodies, plane, dt, iter_mult=4, units=None):
     else:
         found = colliders_ref.collide_units(bodies, plane, units)
     contacts = [contact_ref.Contact(b0, b1, p, n, pen) for b0, b1, p, n, pen in found]
-    pos_used, vel_used = contact_ref.resolve_contacts(len(contacts) * iter_mult, contacts, bodies, dt)
+    pos_used, vel_used = contact_ref.resolve_contacts(len(contacts) * iter_mult, contacts, bodies, dt, trace)
     return len(contacts), pos_used, vel_used
