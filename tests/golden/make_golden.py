@@ -1,6 +1,8 @@
-"""Writes the golden fixtures of tests/golden/ from the oracle (the float64
-restatement of the reference's path), for the tests and for a later run of
-the reference itself where a Go toolchain exists.
+"""Writes the golden fixtures of tests/golden/ from the oracle (the
+restatement of the reference's path: float64, and for the *_precision
+fixtures its float32 instantiation with the float64 islands), for the tests
+and, for the float64 ones, for a later run of the reference itself where a Go
+toolchain exists.
 
     python tests/golden/make_golden.py
 
@@ -22,7 +24,7 @@ if ROOT not in sys.path:
 import numpy as np  # noqa: E402
 
 from cubez_gb300 import scenes  # noqa: E402
-from oracle.oracle import FP64, OracleBatch  # noqa: E402
+from oracle.oracle import FP32, FP64, OracleBatch  # noqa: E402
 
 DT = 1.0 / 60.0
 STATE = ("position", "orientation", "velocity", "rotation")
@@ -36,6 +38,12 @@ FIXTURES = {
     # colliders with Offsets (some scaled) in the cubedrop loop
     "offsets_seed73": {"scene": ("offsets", {"num_worlds": 1, "bodies": 14, "seed": 73, "nonrigid": 0.3}),
                        "loop": "cubedrop", "frames": [1, 60, 150]},
+    # the precision form: a world of the bench scene (16 spheres + 16 cubes)
+    # and the cubedrop scene, in float32 with the float64 islands
+    "precision_seed3_precision": {"scene": ("precision", {"num_worlds": 1, "seed": 3}), "loop": "cubedrop",
+                                  "frames": [1, 30, 120, 300], "form": FP32},
+    "cubedrop_seed1_precision": {"scene": ("cubedrop", {"seed": 1}), "loop": "cubedrop", "frames": [1, 60, 240],
+                                 "form": FP32},
 }
 
 
@@ -47,7 +55,7 @@ def build_scene(spec):
 def run(spec):
     """Frames of the fixture's loop on the oracle: {frame: (contacts, state)}."""
     sc = build_scene(spec["scene"])
-    o = OracleBatch(sc, form=FP64)
+    o = OracleBatch(sc, form=spec.get("form", FP64))
     units = scenes.ballistic_units(int(sc.counts[0])) if spec["loop"] == "ballistic" else None
     out = {}
     for fr in range(1, max(spec["frames"]) + 1):
@@ -72,7 +80,9 @@ def main():
     for name, spec in FIXTURES.items():
         sc, out = run(spec)
         doc = {"scene": {"generator": spec["scene"][0], "args": spec["scene"][1]}, "loop": spec["loop"],
-               "dt": float.hex(DT), "form": "float64", "pow_dt": damping_powers(sc),
+               "dt": float.hex(DT),
+               "form": "float64" if spec.get("form", FP64) == FP64 else "float32 with float64 islands",
+               "pow_dt": damping_powers(sc),
                "frames": {str(fr): {"contacts": c, **{k: [[float.hex(float(x)) for x in row] for row in st[k]]
                                                       for k in STATE}}
                           for fr, (c, st) in out.items()}}

@@ -1,6 +1,7 @@
 """The oracle against the committed golden fixtures (tests/golden/*.json,
 written by tests/golden/make_golden.py): the cubedrop and ballistic frame
-loops and colliders with Offsets, float64, bit for bit at the listed frames.
+loops and colliders with Offsets in float64, and a bench-scene world and the
+cubedrop scene in the precision form, bit for bit at the listed frames.
 
 The fixtures pin the oracle between changes; the GPU path is compared with
 the oracle itself by the parity tests.  The path's only libm values are the
