@@ -10,7 +10,9 @@ CPU, lane by lane, as the kernels compute it (CPU only):
   below the lane) for G = 8, 16, 32: each group's list holds exactly its
   world's touching contacts, in contact order;
 * apply_velocity_change_spread's lane map (c = gl % 3, i = gl / 3) and the
-  cross product's component c = a_p b_q - a_q b_p against cross().
+  cross product's component c = a_p b_q - a_q b_p against cross();
+* k_reorder's counting sort: a permutation of the worlds by descending
+  cost, the warm start's worlds first when it is on.
 
 Every contact's position in the reference's order depends on these, and the
 GPU parity tests check the results bit for bit; these checks pin the index
@@ -188,3 +190,37 @@ def test_spread_velocity_change_lane_map():
             i = gl // 3
             t0 = 3 * (i if gl < 6 else 0)
             assert t0 in (0, 3)
+
+
+def reorder(pos_it, vel_it, plain_next=None, buckets=2048):
+    """k_reorder's counting sort: worlds by last frame's iterations,
+    descending; with the warm start on, the worlds it will serve
+    (plain_next == 0) first.  Order within a bucket is free."""
+    key = np.minimum(np.asarray(pos_it) + np.asarray(vel_it), buckets - 1)
+    if plain_next is not None:
+        key = np.where(np.asarray(plain_next) == 0, buckets - 1, key)
+    hist = np.bincount(buckets - 1 - key, minlength=buckets)
+    start = np.concatenate([[0], np.cumsum(hist)[:-1]])
+    order = np.full(len(key), -1)
+    for w in range(len(key)):
+        b = buckets - 1 - key[w]
+        order[start[b]] = w
+        start[b] += 1
+    return order, key
+
+
+def test_reorder_is_a_permutation_by_descending_cost_warm_first():
+    rng = np.random.default_rng(11)
+    for warm in (False, True):
+        W = 5000
+        pos, vel = rng.integers(0, 300, W), rng.integers(0, 3000, W)
+        plain_next = rng.integers(0, 2, W) if warm else None
+        order, key = reorder(pos, vel, plain_next)
+        assert sorted(order.tolist()) == list(range(W))
+        k = key[order]
+        assert np.all(k[:-1] >= k[1:])
+        if warm:
+            served = plain_next[order] == 0
+            # every world the warm start serves precedes every other with a lower key
+            first_plain = np.argmax(~served) if (~served).any() else W
+            assert served[:first_plain].all()
