@@ -3,18 +3,20 @@
 // One warp holds 32 / G worlds; the G lanes of a group own one world.  Within
 // a group the contacts are lane-strided: the argmax is a G-lane butterfly
 // (warp reductions for G = 32) whose tie-break is the reference's
-// first-maximum rule, and the
-// per-iteration update of every contact touching the two resolved bodies is
-// lane-parallel.  The sequential part of an iteration (applyPositionChange
-// on lanes 0 and 1, one body each; applyVelocityChange on the group leader)
-// runs for all groups at once, so each instruction of that chain serves
-// 32 / G worlds: on GB300 a float64 warp instruction costs the same pipe time
-// whatever its active mask, so packing worlds into a warp divides the float64
-// cost of the plain form and of the precision form's islands by 32 / G; with
-// 16 or 32 lanes per world the precision form's position island is spread
-// over 14 lanes of the group instead (apply_position_change).  The friction
-// solve's matrices do not change during adjustVelocities and are computed
-// once per contact, off the chain (friction_prepare).
+// first-maximum rule, and the per-iteration update of every contact touching
+// the two resolved bodies is lane-parallel (gathered to those contacts in the
+// float64 form).  The sequential part of an iteration (applyPositionChange
+// on lanes 0 and 1, one body each; applyVelocityChange on the group leader,
+// or on six lanes in the float64 form) runs for all groups at once, so each
+// instruction of that chain serves 32 / G worlds: on GB300 a float64 warp
+// instruction costs the same pipe time whatever its active mask, so packing
+// worlds into a warp divides the float64 cost of the plain form and of the
+// precision form's islands by 32 / G; with 16 or 32 lanes per world the
+// position and orientation updates are spread over 14 lanes of the group as
+// well (apply_position_change).  The friction solve's matrices do not change
+// during adjustVelocities and are computed once per contact, off the chain
+// (friction_prepare).  With one world per warp in float32 a CTA runs four
+// independent warps (rs_wpc).
 //
 // Groups of a warp advance in lockstep rounds; a group whose world is done
 // idles until the warp's last world finishes its phase.  Worlds are queued in
